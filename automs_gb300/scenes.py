@@ -1,0 +1,206 @@
+"""Seeded synthetic scenes and the binary-STL scene reader.
+
+The generators stand in for the reference's own scene (stl/4321 of the
+reference tree): shoebox rooms with axis-aligned box obstacles, uniform
+linear Tx arrays and planar Rx grids, all float32, seeded with
+numpy.random.Generator(PCG64(seed)).
+
+Scene arrays follow the reference op's layout (go.py:679-737):
+  tris      float32 [N_tri, 3, 3]   (scene_buffer reshaped)
+  mat       int32   [N_tri]
+  mat_prop  float32 [n_mat, 19]     (negative = penetrable)
+"""
+import os
+import struct
+
+import numpy as np
+
+WAVE_LEN_60GHZ = 3e8 / 60e9  # go.py:1343
+
+
+def _quad_grid(p0, u, v, nu, nv):
+    """Triangles of a planar quad p0 + s*u + t*v, s,t in [0,1], split into
+    nu x nv cells of two triangles each."""
+    tris = []
+    for i in range(nu):
+        for j in range(nv):
+            a = p0 + u * (i / nu) + v * (j / nv)
+            b = p0 + u * ((i + 1) / nu) + v * (j / nv)
+            c = p0 + u * ((i + 1) / nu) + v * ((j + 1) / nv)
+            d = p0 + u * (i / nu) + v * ((j + 1) / nv)
+            tris.append([a, b, c])
+            tris.append([a, c, d])
+    return tris
+
+
+def box_tris(lo, hi, n=1):
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    ex = np.array([hi[0] - lo[0], 0, 0])
+    ey = np.array([0, hi[1] - lo[1], 0])
+    ez = np.array([0, 0, hi[2] - lo[2]])
+    tris = []
+    tris += _quad_grid(lo, ex, ey, n, n)            # bottom
+    tris += _quad_grid(lo + ez, ex, ey, n, n)       # top
+    tris += _quad_grid(lo, ex, ez, n, n)            # y = lo
+    tris += _quad_grid(lo + ey, ex, ez, n, n)       # y = hi
+    tris += _quad_grid(lo, ey, ez, n, n)            # x = lo
+    tris += _quad_grid(lo + ex, ey, ez, n, n)       # x = hi
+    return tris
+
+
+def shoebox_scene(n_boxes=20, room=(12.0, 8.0, 3.0), box_tess=3, room_tess=1,
+                  seed=0, keep_clear=()):
+    """Shoebox room [0,X]x[0,Y]x[0,Z] with n_boxes floor-standing boxes.
+
+    Box footprints U[0.2,1.5]^2, heights U[0.3,2.0], centres uniform in the
+    room and clipped to it; boxes that would contain a point of keep_clear
+    (e.g. the Tx position) are redrawn.  Materials: floor, ceiling, walls and
+    one per box, each with a reflection coefficient U[0.3,0.7] over all 19
+    angle bins (non-penetrable)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    X, Y, Z = room
+    tris, mats = [], []
+    props = [rng.uniform(0.3, 0.7) for _ in range(3)]
+    origin = np.zeros(3)
+    ex, ey, ez = np.array([X, 0, 0.0]), np.array([0, Y, 0.0]), np.array([0, 0, Z])
+    floor = _quad_grid(origin, ex, ey, room_tess, room_tess)
+    ceil = _quad_grid(origin + ez, ex, ey, room_tess, room_tess)
+    walls = (_quad_grid(origin, ex, ez, room_tess, room_tess)
+             + _quad_grid(origin + ey, ex, ez, room_tess, room_tess)
+             + _quad_grid(origin, ey, ez, room_tess, room_tess)
+             + _quad_grid(origin + ex, ey, ez, room_tess, room_tess))
+    for group, m in ((floor, 0), (ceil, 1), (walls, 2)):
+        tris += group
+        mats += [m] * len(group)
+    clear = [np.asarray(p, np.float64) for p in keep_clear]
+    for b in range(n_boxes):
+        while True:
+            sx, sy = rng.uniform(0.2, 1.5, size=2)
+            h = rng.uniform(0.3, 2.0)
+            cx, cy = rng.uniform(0, X), rng.uniform(0, Y)
+            lo = np.array([max(cx - sx / 2, 0.0), max(cy - sy / 2, 0.0), 0.0])
+            hi = np.array([min(cx + sx / 2, X), min(cy + sy / 2, Y), min(h, Z)])
+            if all(not (np.all(p >= lo - 0.05) and np.all(p <= hi + 0.05)) for p in clear):
+                break
+        bt = box_tris(lo, hi, box_tess)
+        tris += bt
+        mats += [3 + b] * len(bt)
+        props.append(rng.uniform(0.3, 0.7))
+    tris = np.asarray(tris, np.float32)
+    mat = np.asarray(mats, np.int32)
+    mat_prop = np.repeat(np.asarray(props, np.float32)[:, None], 19, axis=1)
+    return tris, mat, mat_prop
+
+
+def ula(center, axis, n, spacing):
+    """Uniform linear array as [1, n, 3] float32 (go.py stores arrays 2-D)."""
+    center = np.asarray(center, np.float64)
+    axis = np.asarray(axis, np.float64)
+    axis = axis / np.linalg.norm(axis)
+    k = np.arange(n) - (n - 1) / 2
+    return (center[None, :] + k[:, None] * spacing * axis[None, :]).astype(np.float32)[None]
+
+
+def rx_grid(x0, x1, nx, y0, y1, ny, z):
+    """Planar Rx grid [nx, ny, 3] float32 like gen_pos_from_endpoint."""
+    xs = np.linspace(x0, x1, nx, dtype=np.float32)
+    ys = np.linspace(y0, y1, ny, dtype=np.float32)
+    g = np.stack(np.meshgrid(xs, ys, indexing="ij"), axis=-1)
+    zz = np.full(g.shape[:2] + (1,), z, np.float32)
+    return np.concatenate([g, zz], axis=-1).astype(np.float32)
+
+
+def coverage_config(name="coverage-128", seed=0):
+    """Named coverage workloads.
+
+    coverage-128: 12x8x3 m room, 20 boxes (2172 triangles), 16-element ULA at
+      (6, 0.5, 2.5) facing +y, 128x128 Rx grid at z=1.5, 1000x1000 launch,
+      2 reflections.
+    coverage-small: the same room with 4 boxes, 4 Tx, 24x24 Rx, 96x96 launch
+      (sized for the oracle).
+    """
+    lam = WAVE_LEN_60GHZ
+    tx_pos = (6.0, 0.5, 2.5)
+    if name == "coverage-128":
+        tris, mat, mat_prop = shoebox_scene(20, seed=seed, keep_clear=[tx_pos])
+        src = ula(tx_pos, (1, 0, 0), 16, lam / 2)
+        dst = rx_grid(0.25, 11.75, 128, 0.25, 7.75, 128, 1.5)
+        lx = ly = 1000
+        L = 2
+    elif name == "coverage-small":
+        tris, mat, mat_prop = shoebox_scene(4, box_tess=1, seed=seed, keep_clear=[tx_pos])
+        src = ula(tx_pos, (1, 0, 0), 4, lam / 2)
+        dst = rx_grid(0.25, 11.75, 24, 0.25, 7.75, 24, 1.5)
+        lx = ly = 96
+        L = 2
+    elif name == "coverage-tiny":
+        tris, mat, mat_prop = shoebox_scene(2, box_tess=1, seed=seed, keep_clear=[tx_pos])
+        src = ula(tx_pos, (1, 0, 0), 2, lam / 2)
+        dst = rx_grid(0.25, 11.75, 12, 0.25, 7.75, 12, 1.5)
+        lx = ly = 48
+        L = 2
+    else:
+        raise ValueError(name)
+    params = dict(samples_per_launch=1, launch_x=lx, launch_y=ly, wave_len=lam,
+                  max_reflection=L, reserve_size=100, src_bptype=2, dst_bptype=0,
+                  dst_gridsize=5, src_r=0.5e-5, dst_r=0.06,
+                  src_dir=[0.0, 1.0, 0.0], dst_dir=[0.0, 0.0, 0.0])
+    return dict(tris=tris, mat=mat, mat_prop=mat_prop, src=src, dst=dst, params=params)
+
+
+# ----------------------------------------------------------- STL scenes
+def read_stl(path):
+    """Binary STL triangles as float32 [N, 3, 3] (what numpy-stl's
+    mesh.vectors gives, go.py:700-705)."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if len(data) < 84:
+        raise ValueError(f"{path}: too short for binary STL")
+    (n,) = struct.unpack_from("<I", data, 80)
+    if 84 + 50 * n != len(data):
+        raise ValueError(f"{path}: size does not match {n} triangles")
+    rec = np.frombuffer(data, dtype=np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)),
+                                              ("a", "<u2")]), count=n, offset=84)
+    return np.ascontiguousarray(rec["v"], dtype=np.float32)
+
+
+def read_mat(path):
+    names, props = [], []
+    with open(path) as f:
+        for line in f:
+            vals = line.split()
+            if not vals:
+                continue
+            names.append(vals[0])
+            props.append([float(x) for x in vals[1:]])
+    return names, np.asarray(props, np.float32)
+
+
+def load_scene_folder(folder, blackhole_buffer=(), reflector_buffer=(), door_buffer=()):
+    """Scene ingest of build_channel (go.py:679-737): every *.stl in the
+    folder (material from the file-name suffix), then pseudo-materials
+    blackhole (0), reflector (1) and door (-0.7) for the extra quads."""
+    names, props = read_mat(os.path.join(folder, "mat.txt"))
+    props = [list(p) for p in props]
+    tris, mats = [], []
+    for fn in os.listdir(folder):  # os.listdir order, as the reference
+        if not fn.endswith(".stl"):
+            continue
+        v = read_stl(os.path.join(folder, fn))
+        mat_name = fn.split("_")[-1].split(".stl")[0]
+        mid = names.index(mat_name)
+        tris.append(v)
+        mats.append(np.full(v.shape[0], mid, np.int32))
+    for buf, val, label in ((blackhole_buffer, 0.0, "blackhole"),
+                            (reflector_buffer, 1.0, "reflector"),
+                            (door_buffer, -0.7, "door")):
+        if len(buf) > 0:
+            props.append([val] * 19)
+            t = np.asarray([tri for quad in buf for tri in quad], np.float32).reshape(-1, 3, 3)
+            tris.append(t)
+            mats.append(np.full(t.shape[0], len(names), np.int32))
+            names.append(label)
+    tris = np.concatenate(tris, 0) if tris else np.zeros((0, 3, 3), np.float32)
+    mat = np.concatenate(mats, 0) if mats else np.zeros((0,), np.int32)
+    return tris.astype(np.float32), mat, np.asarray(props, np.float32)

@@ -1,0 +1,192 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+Run in a container where the reference tree is mounted (default
+/root/reference, override with AMS_REFERENCE_ROOT):
+
+    python tests/golden/make_golden.py
+
+Two sources:
+  * channel fixtures: the reference's own device programs
+    (optixPathTracer.cu) compiled for the CPU by oracle/ref_harness and run
+    on seeded synthetic scenes (cases in tests/golden/cases.py);
+  * objective fixtures: the reference's own go.Model (go.py:27-245) imported
+    with stub matplotlib / numpy-stl modules and run on the CPU, loss and
+    autograd gradients recorded.
+Outputs are small .npz files; the inputs are regenerated from the case
+definitions, whose sha256 is stored alongside to catch generator drift.
+"""
+import contextlib
+import ctypes as C
+import hashlib
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, HERE)
+REF = os.environ.get("AMS_REFERENCE_ROOT", "/root/reference")
+
+import cases  # noqa: E402
+import oracle  # noqa: E402
+
+
+def digest(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def make_channel_fixtures():
+    for name in cases.CHANNEL_CASES:
+        c = cases.channel_case(name)
+        H, st, paths = oracle.ref_trace_channel(c["tris"], c["mat"], c["mat_prop"],
+                                                c["src"], c["dst"], c["params"])
+        np.savez_compressed(
+            os.path.join(HERE, f"chan_{name}.npz"),
+            H=H, paths=paths,
+            stats=np.array([st[k] for k in cases.STAT_KEYS], np.int64),
+            input_sha=np.array(digest(c["tris"], c["mat"], c["mat_prop"], c["src"], c["dst"])))
+        print(name, st)
+
+
+def make_unit_fixtures():
+    R = oracle.ref_lib()
+    rng = np.random.Generator(np.random.PCG64(7))
+    seeds = rng.integers(0, 2**32, size=256, dtype=np.uint64).astype(np.uint32)
+    tea = np.array([R.ref_tea4(int(s), 0) for s in seeds], np.uint32)
+    rnd_seq = []
+    for s in seeds[:32]:
+        st = C.c_uint32(int(s))
+        rnd_seq.append([R.ref_rnd(C.byref(st)) for _ in range(16)])
+    rnd_seq = np.array(rnd_seq, np.float32)
+    dirs = []
+    rd_in = []
+    for k in range(512):
+        lx, ly = int(rng.integers(1, 1200)), int(rng.integers(1, 1200))
+        ix, iy = int(rng.integers(0, lx)), int(rng.integers(0, ly))
+        st = C.c_uint32(R.ref_tea4(ix * ly + iy, 0))
+        R.ref_rnd(C.byref(st))  # the src draw precedes the direction
+        out = np.zeros(3, np.float32)
+        R.ref_rand_dir(C.byref(st), ix, iy, lx, ly, out)
+        dirs.append(out)
+        rd_in.append([ix, iy, lx, ly])
+    d1 = rng.normal(size=(400, 3)).astype(np.float32)
+    d2 = rng.normal(size=(400, 3)).astype(np.float32)
+    bp = np.zeros((400, 4), np.float32)
+    for i in range(400):
+        for t in range(4):
+            bp[i, t] = R.ref_beampattern(np.ascontiguousarray(d1[i]), np.ascontiguousarray(d2[i]), t)
+    n = rng.normal(size=(200, 3)).astype(np.float32)
+    n /= np.linalg.norm(n, axis=1, keepdims=True)
+    n = n.astype(np.float32)
+    a = rng.uniform(-5, 5, size=(200, 3)).astype(np.float32)
+    m0 = rng.uniform(-2, 2, size=(200, 12)).astype(np.float32)
+    m1 = m0.copy()
+    for i in range(200):
+        row = np.ascontiguousarray(m1[i])
+        R.ref_image_update(row, np.ascontiguousarray(n[i]), np.ascontiguousarray(a[i]))
+        m1[i] = row
+    cosv = rng.uniform(-1, 1, size=4000).astype(np.float32)
+    tid = np.array([R.ref_theta_id(float(c)) for c in cosv], np.int32)
+    np.savez_compressed(os.path.join(HERE, "unit_ref.npz"), seeds=seeds, tea=tea,
+                        rnd_seq=rnd_seq, rand_dir=np.array(dirs, np.float32),
+                        rand_dir_in=np.array(rd_in, np.int64), bp_d1=d1, bp_d2=d2, bp=bp,
+                        img_n=n, img_a=a, img_m0=m0, img_m1=m1, theta_cos=cosv, theta_id=tid)
+    print("unit fixtures written")
+
+
+# ------------------------------------------------------------ objective
+@contextlib.contextmanager
+def reference_go_on_cpu():
+    """Import the reference go.py with stub plotting / STL modules and with
+    its hard-coded device="cuda" redirected to the CPU."""
+    import torch
+    stubs = {}
+    for name in ("matplotlib", "matplotlib.pyplot", "stl", "stl.mesh"):
+        stubs[name] = types.ModuleType(name)
+    stubs["stl"].mesh = stubs["stl.mesh"]
+    stubs["matplotlib"].pyplot = stubs["matplotlib.pyplot"]
+    saved_mods = {k: sys.modules.get(k) for k in stubs}
+    sys.modules.update(stubs)
+    factories = ("ones", "zeros", "rand", "tensor", "linspace")
+    saved = {f: getattr(torch, f) for f in factories}
+
+    def wrap(fn):
+        def inner(*a, **kw):
+            if kw.get("device") == "cuda":
+                kw["device"] = "cpu"
+            return fn(*a, **kw)
+        return inner
+    for f in factories:
+        setattr(torch, f, wrap(saved[f]))
+    sys.path.insert(0, REF)
+    try:
+        import go  # the reference module
+        yield go, saved
+    finally:
+        sys.path.remove(REF)
+        for f in factories:
+            setattr(torch, f, saved[f])
+        for k, v in saved_mods.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+
+
+def make_objective_fixtures():
+    import torch
+    with reference_go_on_cpu() as (go, saved):
+        for name in cases.OBJECTIVE_CASES:
+            c = cases.objective_case(name)
+            chans = {k: torch.from_numpy(v) for k, v in c["channels"].items()}
+            ms_list = [go.Metasurface(None, None, None, None, None, c["max_phase_deg"])
+                       for _ in range(c["n_ms"])]
+            model = go.Model(name, channels=chans, ms_list=ms_list,
+                             max_ms_reflex=c["max_ms_reflex"], code_num=c["code_num"], w=c["w"])
+            with torch.no_grad():
+                model.antenna_theta.copy_(torch.from_numpy(c["theta"]))
+                for i in range(c["n_ms"]):
+                    model.ms_theta[i].copy_(torch.from_numpy(c["phi"][i]))
+            mask_box = {}
+            real_rand = torch.rand  # the device-redirecting wrapper
+
+            def rand_hook(*a, **kw):
+                out = real_rand(*a, **kw)
+                mask_box["r"] = out.clone()
+                return out
+            torch.manual_seed(c["seed"])
+            torch.rand = rand_hook
+            try:
+                loss = model.forward()
+            finally:
+                torch.rand = real_rand
+            for p in model.parameters():
+                p.grad = None
+            loss.backward()
+            drop = (mask_box["r"] < 0.1).numpy()
+            out = dict(loss=np.float64(loss.item()), drop=drop,
+                       recv_amp=model.result.numpy(), cap=model.cap.numpy(),
+                       grad_theta=model.antenna_theta.grad.numpy())
+            for i in range(c["n_ms"]):
+                g = model.ms_theta[i].grad
+                out[f"grad_phi{i}"] = (g.numpy() if g is not None
+                                       else np.zeros_like(c["phi"][i]))
+            out["input_sha"] = np.array(digest(*[c["channels"][k] for k in sorted(c["channels"])],
+                                               c["theta"], *c["phi"]))
+            np.savez_compressed(os.path.join(HERE, f"obj_{name}.npz"), **out)
+            print(name, "loss", loss.item(), "dropped rows", int(drop.sum()))
+
+
+if __name__ == "__main__":
+    if not oracle.ref_available():
+        raise SystemExit("reference tree not mounted; fixtures cannot be regenerated here")
+    make_unit_fixtures()
+    make_channel_fixtures()
+    make_objective_fixtures()
