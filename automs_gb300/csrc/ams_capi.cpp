@@ -1,0 +1,577 @@
+// ams_capi.cpp -- host orchestration behind the C ABI of include/ams.h.
+//
+// Replaces optixPathTracer.cpp:70-360 (launch parameters, two-stage launch,
+// host dedup and flood-fill scheduler) and :781-870 (the Torch op):
+//   * the triangle BVH is built once per scene and kept across calls;
+//   * the Tx/Rx sphere BVHs, path table and bitmaps live in one device
+//     workspace per scene that grows to the largest call and is reused;
+//   * the host loop only reads a handful of device counters per round;
+//   * every failure is returned as a status with a message.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ams.h"
+#include "lbvh.h"
+#include "trace.h"
+
+namespace {
+
+void set_err(char *buf, size_t len, const char *fmt, ...) {
+  if (!buf || len == 0) return;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, len, fmt, ap);
+  va_end(ap);
+}
+
+struct Arena {
+  char *base = nullptr;
+  size_t cap = 0, used = 0, high = 0;
+  ~Arena() { if (base) cudaFree(base); }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (base) { cudaFree(base); base = nullptr; cap = 0; }
+    cudaError_t e = cudaMalloc(&base, bytes);
+    if (e != cudaSuccess) { base = nullptr; return e; }
+    cap = bytes;
+    high = std::max(high, bytes);
+    return cudaSuccess;
+  }
+  void reset() { used = 0; }
+  template <class T> T *take(size_t count) {
+    size_t b = (sizeof(T) * count + 255) & ~(size_t)255;
+    T *p = reinterpret_cast<T *>(base + used);
+    used += b;
+    return p;
+  }
+};
+
+size_t al(size_t v) { return (v + 255) & ~(size_t)255; }
+
+struct HostCounters {
+  unsigned long long ctr[16];
+  unsigned err;
+};
+
+}  // namespace
+
+struct ams_scene {
+  int device = 0;
+  int n_tri = 0, n_mat = 0;
+  float *tris = nullptr;
+  int *mat = nullptr;
+  float *mat_prop = nullptr;
+  char *bvh_out = nullptr;
+  Lbvh bvh;
+  Arena ws;       // per-call workspace
+  Arena tasks;    // task list of a round (grown on demand)
+  int tab_log2 = 14;
+  HostCounters *hc = nullptr;  // pinned
+  TraceDev last{};
+  bool have_last = false;
+  float ms_bvh_scene = 0.f;
+  cudaEvent_t k2[2] = {nullptr, nullptr};
+  ~ams_scene() {
+    for (auto &e : k2)
+      if (e) cudaEventDestroy(e);
+    if (tris) cudaFree(tris);
+    if (mat) cudaFree(mat);
+    if (mat_prop) cudaFree(mat_prop);
+    if (bvh_out) cudaFree(bvh_out);
+    if (hc) cudaFreeHost(hc);
+  }
+};
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t _e = (call);                                                             \
+    if (_e != cudaSuccess) {                                                             \
+      set_err(errbuf, errlen, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(_e),   \
+              __FILE__, __LINE__);                                                       \
+      return _e == cudaErrorMemoryAllocation ? AMS_ERR_OOM : AMS_ERR_CUDA;               \
+    }                                                                                    \
+  } while (0)
+
+extern "C" {
+
+const char *ams_version(void) { return "automs-gb300 0.1 (sm_103a)"; }
+
+ams_status ams_scene_create(const float *tris, int n_tri, const int *mat, const float *mat_prop,
+                            int n_mat, void *stream, ams_scene **out, char *errbuf,
+                            size_t errlen) {
+  if (!out) { set_err(errbuf, errlen, "out is NULL"); return AMS_ERR_ARG; }
+  *out = nullptr;
+  if (n_tri < 0 || n_mat < 0 || (n_tri > 0 && (!tris || !mat)) || (n_mat > 0 && !mat_prop) ||
+      (n_tri > 0 && n_mat == 0)) {
+    set_err(errbuf, errlen, "bad scene arrays (n_tri=%d, n_mat=%d)", n_tri, n_mat);
+    return AMS_ERR_ARG;
+  }
+  if (n_tri > (1 << 28)) { set_err(errbuf, errlen, "too many triangles"); return AMS_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  ams_scene *s = new ams_scene();
+  cudaGetDevice(&s->device);
+  s->n_tri = n_tri;
+  s->n_mat = n_mat;
+  auto fail = [&](ams_status code) { delete s; return code; };
+  cudaError_t e;
+  if ((e = cudaEventCreate(&s->k2[0])) != cudaSuccess || (e = cudaEventCreate(&s->k2[1])) != cudaSuccess ||
+      (e = cudaMallocHost(&s->hc, sizeof(HostCounters))) != cudaSuccess) {
+    set_err(errbuf, errlen, "cudaMallocHost: %s", cudaGetErrorString(e));
+    return fail(AMS_ERR_OOM);
+  }
+  size_t tb = sizeof(float) * 9 * (size_t)std::max(n_tri, 1);
+  if ((e = cudaMalloc(&s->tris, tb)) != cudaSuccess ||
+      (e = cudaMalloc(&s->mat, sizeof(int) * (size_t)std::max(n_tri, 1))) != cudaSuccess ||
+      (e = cudaMalloc(&s->mat_prop, sizeof(float) * 19 * (size_t)std::max(n_mat, 1))) !=
+          cudaSuccess ||
+      (e = cudaMalloc(&s->bvh_out, lbvh_output_bytes(n_tri))) != cudaSuccess) {
+    set_err(errbuf, errlen, "scene allocation: %s", cudaGetErrorString(e));
+    return fail(AMS_ERR_OOM);
+  }
+  if (n_tri > 0) {
+    // material ids index mat_prop rows: check them on the host once
+    std::vector<int> hm((size_t)n_tri);
+    if ((e = cudaMemcpy(hm.data(), mat, sizeof(int) * (size_t)n_tri, cudaMemcpyDeviceToHost)) !=
+        cudaSuccess) {
+      set_err(errbuf, errlen, "reading mat: %s", cudaGetErrorString(e));
+      return fail(AMS_ERR_CUDA);
+    }
+    for (int i = 0; i < n_tri; i++)
+      if (hm[i] < 0 || hm[i] >= n_mat) {
+        set_err(errbuf, errlen, "mat[%d] = %d is outside [0, %d)", i, hm[i], n_mat);
+        return fail(AMS_ERR_ARG);
+      }
+    cudaMemcpyAsync(s->tris, tris, sizeof(float) * 9 * (size_t)n_tri, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(s->mat, mat, sizeof(int) * (size_t)n_tri, cudaMemcpyDeviceToDevice, st);
+  }
+  if (n_mat > 0)
+    cudaMemcpyAsync(s->mat_prop, mat_prop, sizeof(float) * 19 * (size_t)n_mat,
+                    cudaMemcpyDeviceToDevice, st);
+  if ((e = s->ws.ensure(lbvh_scratch_bytes(n_tri) + 1024)) != cudaSuccess) {
+    set_err(errbuf, errlen, "BVH scratch: %s", cudaGetErrorString(e));
+    return fail(AMS_ERR_OOM);
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  if ((e = lbvh_build_triangles(s->bvh, s->tris, n_tri, s->ws.base, s->bvh_out, st)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+    set_err(errbuf, errlen, "triangle BVH build: %s", cudaGetErrorString(e));
+    return fail(AMS_ERR_CUDA);
+  }
+  s->ms_bvh_scene =
+      std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  *out = s;
+  return AMS_OK;
+}
+
+void ams_scene_destroy(ams_scene *scene) { delete scene; }
+
+static ams_status validate(const ams_trace_params *p, int s0, int s1, int n0, int n1,
+                           char *errbuf, size_t errlen) {
+  if (!p) { set_err(errbuf, errlen, "params is NULL"); return AMS_ERR_ARG; }
+  if (s0 <= 0 || s1 <= 0 || n0 <= 0 || n1 <= 0) {
+    set_err(errbuf, errlen, "empty src or dst array");
+    return AMS_ERR_ARG;
+  }
+  if ((long long)s0 * s1 > (1 << 26) || (long long)n0 * n1 > (1 << 28)) {
+    set_err(errbuf, errlen, "src/dst arrays too large");
+    return AMS_ERR_ARG;
+  }
+  if (p->max_reflection < 0 || p->max_reflection > 5) {
+    set_err(errbuf, errlen, "max_reflection must be in [0, 5] (32 branch slots), got %d",
+            p->max_reflection);
+    return AMS_ERR_ARG;
+  }
+  if (p->reserve_size < 1 || p->reserve_size > 256) {
+    set_err(errbuf, errlen, "reserve_size must be in [1, 256], got %d", p->reserve_size);
+    return AMS_ERR_ARG;
+  }
+  if (p->samples_per_launch < 0 || p->launch_x <= 0 || p->launch_y <= 0 ||
+      (long long)p->launch_x * p->launch_y > (1LL << 31) - 1) {
+    set_err(errbuf, errlen, "bad launch grid");
+    return AMS_ERR_ARG;
+  }
+  if (p->src_bptype < 0 || p->src_bptype > 3 || p->dst_bptype < 0 || p->dst_bptype > 3) {
+    set_err(errbuf, errlen, "beam pattern types must be in [0, 3]");
+    return AMS_ERR_ARG;
+  }
+  if (p->dst_gridsize <= 0) { set_err(errbuf, errlen, "dst_gridsize must be > 0"); return AMS_ERR_ARG; }
+  if (!(p->wave_len > 0.0)) { set_err(errbuf, errlen, "wave_len must be > 0"); return AMS_ERR_ARG; }
+  if (!(p->src_r >= 0.f) || !(p->dst_r >= 0.f)) {
+    set_err(errbuf, errlen, "radii must be >= 0");
+    return AMS_ERR_ARG;
+  }
+  return AMS_OK;
+}
+
+ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const float *src, int s0,
+                             int s1, const float *dst, int n0, int n1, const float *src_aabb_in,
+                             const float *dst_aabb_in, float *result, ams_stats *stats,
+                             void *stream, char *errbuf, size_t errlen) {
+  if (!S) { set_err(errbuf, errlen, "scene is NULL"); return AMS_ERR_ARG; }
+  ams_status v = validate(p, s0, s1, n0, n1, errbuf, errlen);
+  if (v != AMS_OK) return v;
+  if (!src || !dst || !result) { set_err(errbuf, errlen, "null src/dst/result"); return AMS_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n_src = s0 * s1, n_dst = n0 * n1, gs = p->dst_gridsize;
+  const int n0g = (n0 - 1) / gs + 1, n1g = (n1 - 1) / gs + 1, ng = n0g * n1g;
+  cudaEvent_t ev[4];
+  for (auto &e : ev) CK(cudaEventCreate(&e));
+  struct EvGuard { cudaEvent_t *e; ~EvGuard() { for (int i = 0; i < 4; i++) cudaEventDestroy(e[i]); } } eg{ev};
+  CK(cudaEventRecord(ev[0], st));
+
+  for (int attempt = 0; attempt < 6; attempt++) {
+    const unsigned tab_size = 1u << S->tab_log2;
+    const int W = (int)(tab_size / 32);
+    size_t need = 0;
+    need += al(sizeof(float) * 6 * (size_t)n_src) + al(sizeof(float) * 6 * (size_t)n_dst);
+    need += al(std::max(lbvh_scratch_bytes(n_src), lbvh_scratch_bytes(n_dst)));
+    need += al(lbvh_output_bytes(n_src)) + al(lbvh_output_bytes(n_dst));
+    need += al(8 * (size_t)tab_size) + al(4 * (size_t)tab_size) + al(56 * (size_t)tab_size);
+    need += 3 * al(4 * (size_t)ng * W);
+    need += al(16 * (size_t)n_src * n_dst);
+    need += al(8 * 16) + al(4);
+    need += 4096;
+    CK(S->ws.ensure(need));
+    S->ws.reset();
+    const float *src_aabb = src_aabb_in, *dst_aabb = dst_aabb_in;
+    float *sbox = src_aabb ? nullptr : S->ws.take<float>(6 * (size_t)n_src);
+    float *dbox = dst_aabb ? nullptr : S->ws.take<float>(6 * (size_t)n_dst);
+    char *scratch = S->ws.take<char>(std::max(lbvh_scratch_bytes(n_src), lbvh_scratch_bytes(n_dst)));
+    char *tx_out = S->ws.take<char>(lbvh_output_bytes(n_src));
+    char *rx_out = S->ws.take<char>(lbvh_output_bytes(n_dst));
+    TraceDev P{};
+    P.tab_h = S->ws.take<unsigned long long>(tab_size);
+    P.tab_chk = S->ws.take<unsigned>(tab_size);
+    P.tab_key = S->ws.take<int32_t>(14 * (size_t)tab_size);
+    P.T = S->ws.take<unsigned>((size_t)ng * W);
+    P.N = S->ws.take<unsigned>((size_t)ng * W);
+    P.S = S->ws.take<unsigned>((size_t)ng * W);
+    P.acc = S->ws.take<unsigned long long>(2 * (size_t)n_src * n_dst);
+    P.ctr = S->ws.take<unsigned long long>(16);
+    P.err = S->ws.take<unsigned>(1);
+
+    if (!src_aabb) { CK(sphere_aabbs(src, n_src, p->src_r, sbox, st)); src_aabb = sbox; }
+    if (!dst_aabb) { CK(sphere_aabbs(dst, n_dst, p->dst_r, dbox, st)); dst_aabb = dbox; }
+    Lbvh tx, rx;
+    CK(lbvh_build_spheres(tx, src, src_aabb, n_src, scratch, tx_out, st));
+    CK(lbvh_build_spheres(rx, dst, dst_aabb, n_dst, scratch, rx_out, st));
+    CK(cudaEventRecord(ev[1], st));
+
+    P.tris = S->tris;
+    P.tri_nodes = S->bvh.nodes;
+    P.tri_prims = S->bvh.prims;
+    P.n_tri = S->n_tri;
+    P.mat = S->mat;
+    P.mat_prop = S->mat_prop;
+    P.tx_nodes = tx.nodes; P.tx_prims = tx.prims; P.n_src = n_src; P.src = src; P.src_r = p->src_r;
+    P.rx_nodes = rx.nodes; P.rx_prims = rx.prims; P.n_dst = n_dst; P.dst = dst; P.dst_r = p->dst_r;
+    P.n0_dst = n0; P.n1_dst = n1; P.n0g = n0g; P.n1g = n1g; P.ng = ng; P.gs = gs;
+    P.strict_grid = p->strict_grid;
+    P.L = p->max_reflection; P.reserve = p->reserve_size; P.spl = p->samples_per_launch;
+    P.launch_x = p->launch_x; P.launch_y = p->launch_y;
+    P.lam_f = (float)p->wave_len; P.lam_d = p->wave_len;
+    for (int k = 0; k < 3; k++) { P.src_dir[k] = p->src_dir[k]; P.dst_dir[k] = p->dst_dir[k]; }
+    P.src_bp = p->src_bptype; P.dst_bp = p->dst_bptype;
+    P.tab_mask = tab_size - 1;
+    P.tab_limit = tab_size / 2;
+    P.W = W;
+
+    CK(cudaMemsetAsync(P.tab_h, 0, 8 * (size_t)tab_size, st));
+    CK(cudaMemsetAsync(P.tab_chk, 0, 4 * (size_t)tab_size, st));
+    CK(cudaMemsetAsync(P.T, 0, 4 * (size_t)ng * W, st));
+    CK(cudaMemsetAsync(P.S, 0, 4 * (size_t)ng * W, st));
+    CK(cudaMemsetAsync(P.acc, 0, 16 * (size_t)n_src * n_dst, st));
+    CK(cudaMemsetAsync(P.ctr, 0, 8 * 16, st));
+    CK(cudaMemsetAsync(P.err, 0, 4, st));
+
+    // ---- stage 1
+    CK(trace_stage1(P, st));
+    CK(trace_count_bits(P, P.T, P.ctr + 6, st));
+    CK(cudaEventRecord(ev[2], st));
+    CK(cudaMemcpyAsync(S->hc->ctr, P.ctr, 128, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&S->hc->err, P.err, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (S->hc->err & AMS_DERR_PATH_TABLE) {
+      if (S->tab_log2 >= 26) {
+        set_err(errbuf, errlen, "path table would exceed 2^26 slots");
+        return AMS_ERR_CAPACITY;
+      }
+      S->tab_log2 += 2;
+      continue;  // grow the path table and run again
+    }
+    if (S->hc->err) {
+      set_err(errbuf, errlen, "stage 1 device error flags 0x%x", S->hc->err);
+      return (S->hc->err & AMS_DERR_HASH) ? AMS_ERR_INTERNAL : AMS_ERR_CAPACITY;
+    }
+    const unsigned long long fwd_records = S->hc->ctr[0];
+    const unsigned long long overflow = S->hc->ctr[1];
+    const unsigned long long n_paths = S->hc->ctr[2];
+    const unsigned long long unique_records = S->hc->ctr[6];
+
+    // ---- stage 2 rounds
+    unsigned long long rounds = 0, total_tasks = 0;
+    float ms_k2 = 0.f;
+    unsigned long long n_new = unique_records;
+    if (fwd_records > 0) {
+      CK(cudaMemcpyAsync(P.N, P.T, 4 * (size_t)ng * W, cudaMemcpyDeviceToDevice, st));
+      while (n_new > 0) {
+        if (S->tasks.cap < n_new * sizeof(int2)) {
+          CK(cudaStreamSynchronize(st));
+          CK(S->tasks.ensure(std::max<size_t>(n_new * sizeof(int2) * 2, 1 << 20)));
+        }
+        P.tasks = reinterpret_cast<int2 *>(S->tasks.base);
+        P.task_cap = S->tasks.cap / sizeof(int2);
+        CK(cudaMemsetAsync(P.ctr + 5, 0, 8, st));
+        CK(cudaMemsetAsync(P.ctr + 7, 0, 8, st));
+        CK(trace_make_tasks(P, P.N, st));
+        CK(cudaEventRecord(S->k2[0], st));
+        CK(trace_stage2(P, n_new, st));
+        CK(cudaEventRecord(S->k2[1], st));
+        CK(trace_expand(P, st));
+        rounds++;
+        total_tasks += n_new;
+        CK(cudaMemcpyAsync(S->hc->ctr, P.ctr, 128, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&S->hc->err, P.err, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (S->hc->err) {
+          set_err(errbuf, errlen, "stage 2 device error flags 0x%x", S->hc->err);
+          return (S->hc->err & AMS_DERR_ACC_RANGE) ? AMS_ERR_NUMERIC : AMS_ERR_CAPACITY;
+        }
+        float kms = 0.f;
+        cudaEventElapsedTime(&kms, S->k2[0], S->k2[1]);
+        ms_k2 += kms;
+        if (S->hc->ctr[5] != n_new) {
+          set_err(errbuf, errlen, "task count mismatch (%llu listed, %llu expected)",
+                  S->hc->ctr[5], n_new);
+          return AMS_ERR_INTERNAL;
+        }
+        n_new = S->hc->ctr[7];
+      }
+      CK(trace_finalize(P, result, st));
+    }
+    CK(cudaEventRecord(ev[3], st));
+    CK(cudaMemcpyAsync(S->hc->ctr, P.ctr, 128, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    S->last = P;
+    S->have_last = true;
+    if (stats) {
+      memset(stats, 0, sizeof(*stats));
+      stats->rx_paths = S->hc->ctr[3];
+      stats->rx_fail = S->hc->ctr[4];
+      stats->fwd_records = fwd_records;
+      stats->unique_records = fwd_records ? unique_records : 0;
+      stats->unique_paths = fwd_records ? n_paths : 0;
+      stats->rounds = rounds;
+      stats->tasks = total_tasks;
+      stats->overflow = overflow;
+      cudaEventElapsedTime(&stats->ms_bvh, ev[0], ev[1]);
+      cudaEventElapsedTime(&stats->ms_stage1, ev[1], ev[2]);
+      cudaEventElapsedTime(&stats->ms_stage2, ev[2], ev[3]);
+      cudaEventElapsedTime(&stats->ms_total, ev[0], ev[3]);
+      stats->workspace_bytes = S->ws.high + S->tasks.high;
+      stats->segments_fwd = S->hc->ctr[8];
+      stats->segments_bwd = S->hc->ctr[9];
+      stats->ms_stage2_kernel = ms_k2;
+    }
+    if (p->log_level > 0) {
+      float a = 0, b = 0, c = 0;
+      cudaEventElapsedTime(&a, ev[0], ev[1]);
+      cudaEventElapsedTime(&b, ev[1], ev[2]);
+      cudaEventElapsedTime(&c, ev[2], ev[3]);
+      fprintf(stderr,
+              "[ams] bvh %.3f ms, stage1 %.3f ms (%llu records, %llu unique, %llu paths), "
+              "stage2 %.3f ms (%llu rounds, %llu tasks), rays %llu ok / %llu failed\n",
+              a, b, fwd_records, unique_records, n_paths, c, rounds, total_tasks,
+              S->hc->ctr[3], S->hc->ctr[4]);
+    }
+    return AMS_OK;
+  }
+  set_err(errbuf, errlen, "path table retries exhausted");
+  return AMS_ERR_CAPACITY;
+}
+
+ams_status ams_launch_pathtrace(float *result, const float *src, int s0, int s1, const float *dst,
+                                int n0, int n1, const float *src_aabb, const float *dst_aabb,
+                                const float *scene_tris, int n_tri, const int *mat,
+                                int samples_per_launch, int launch_x, int launch_y,
+                                double wave_len, int max_reflection, int reserve_size,
+                                const float *mat_prop, int n_mat, const float *src_dir,
+                                const float *dst_dir, int log_level, int src_bptype,
+                                int dst_bptype, int dst_gridsize, double src_r, double dst_r,
+                                ams_stats *stats, char *errbuf, size_t errlen) {
+  if (!src_dir || !dst_dir) { set_err(errbuf, errlen, "src_dir/dst_dir are NULL"); return AMS_ERR_ARG; }
+  ams_trace_params p{};
+  p.samples_per_launch = samples_per_launch;
+  p.launch_x = launch_x;
+  p.launch_y = launch_y;
+  p.wave_len = wave_len;
+  p.max_reflection = max_reflection;
+  p.reserve_size = reserve_size;
+  p.src_bptype = src_bptype;
+  p.dst_bptype = dst_bptype;
+  p.dst_gridsize = dst_gridsize;
+  p.src_r = (float)src_r;
+  p.dst_r = (float)dst_r;
+  for (int k = 0; k < 3; k++) { p.src_dir[k] = src_dir[k]; p.dst_dir[k] = dst_dir[k]; }
+  p.log_level = log_level;
+  ams_scene *scene = nullptr;
+  ams_status s = ams_scene_create(scene_tris, n_tri, mat, mat_prop, n_mat, nullptr, &scene,
+                                  errbuf, errlen);
+  if (s != AMS_OK) return s;
+  s = ams_trace_channel(scene, &p, src, s0, s1, dst, n0, n1, src_aabb, dst_aabb, result, stats,
+                        nullptr, errbuf, errlen);
+  ams_scene_destroy(scene);
+  return s;
+}
+
+ams_status ams_trace_export_paths(ams_scene *S, int32_t *host_out, int max_paths, int *n_out,
+                                  char *errbuf, size_t errlen) {
+  if (!S || !n_out || (max_paths > 0 && !host_out)) {
+    set_err(errbuf, errlen, "bad arguments");
+    return AMS_ERR_ARG;
+  }
+  *n_out = 0;
+  if (!S->have_last) return AMS_OK;
+  const TraceDev &P = S->last;
+  size_t n = (size_t)P.tab_mask + 1;
+  int32_t *dev = nullptr;
+  unsigned long long *cnt = nullptr;
+  CK(cudaMalloc(&dev, 56 * n + 64));
+  cnt = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(dev) + 56 * n);
+  ams_status rc = AMS_OK;
+  unsigned long long got = 0;
+  if (cudaMemset(cnt, 0, 8) != cudaSuccess || trace_export_paths(P, dev, cnt, nullptr) != cudaSuccess ||
+      cudaMemcpy(&got, cnt, 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+    set_err(errbuf, errlen, "path export failed");
+    rc = AMS_ERR_CUDA;
+  } else {
+    size_t k = std::min<size_t>(got, (size_t)std::max(max_paths, 0));
+    if (k && cudaMemcpy(host_out, dev, 56 * k, cudaMemcpyDeviceToHost) != cudaSuccess) {
+      set_err(errbuf, errlen, "path copy failed");
+      rc = AMS_ERR_CUDA;
+    }
+    *n_out = (int)got;
+  }
+  cudaFree(dev);
+  return rc;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ objective
+#include <mutex>
+#include <vector>
+
+#include "objective.h"
+
+namespace {
+struct DevScratch {
+  char *ptr = nullptr;
+  size_t cap = 0;
+};
+std::mutex g_scratch_mu;
+std::vector<DevScratch> g_scratch;
+
+cudaError_t scratch_for(size_t bytes, char **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  if ((int)g_scratch.size() <= dev) g_scratch.resize(dev + 1);
+  DevScratch &d = g_scratch[dev];
+  if (d.cap < bytes) {
+    // the buffer may still be in use by earlier asynchronous calls
+    if (d.ptr) {
+      if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
+      cudaFree(d.ptr);
+      d.ptr = nullptr;
+      d.cap = 0;
+    }
+    size_t want = std::max(bytes, (size_t)1 << 20);
+    if ((e = cudaMalloc(&d.ptr, want)) != cudaSuccess) return e;
+    d.cap = want;
+  }
+  *out = d.ptr;
+  return cudaSuccess;
+}
+
+ams_status obj_validate(const float *H_d, const float *H_a, const float *H_r, const float *phi,
+                        float max_phase, const float *W, int S, int M, int R, int C,
+                        char *errbuf, size_t errlen) {
+  if (!H_d || !W) { set_err(errbuf, errlen, "H_d and W are required"); return AMS_ERR_ARG; }
+  if (S <= 0 || R <= 0 || C <= 0) {
+    set_err(errbuf, errlen, "S, R and C must be positive (S=%d R=%d C=%d)", S, R, C);
+    return AMS_ERR_ARG;
+  }
+  if (C > 64) { set_err(errbuf, errlen, "at most 64 codes per call (C=%d)", C); return AMS_ERR_ARG; }
+  bool ms = H_a || H_r;
+  if (ms && (!H_a || !H_r || !phi || M <= 0)) {
+    set_err(errbuf, errlen, "metasurface hop needs H_a, H_r, phi and M > 0");
+    return AMS_ERR_ARG;
+  }
+  if (ms && !(max_phase > 0.f)) { set_err(errbuf, errlen, "max_phase must be > 0"); return AMS_ERR_ARG; }
+  return AMS_OK;
+}
+}  // namespace
+
+extern "C" {
+
+ams_status ams_objective_fwd_bwd(const float *H_d, const float *H_a, const float *H_r,
+                                 const float *phi, float max_phase, const float *W, int S, int M,
+                                 int R, int C, float w, const uint8_t *drop, float *loss,
+                                 float *grad_W, float *grad_phi, float *grad_Y, float *recv_amp,
+                                 void *stream, char *errbuf, size_t errlen) {
+  ams_status v = obj_validate(H_d, H_a, H_r, phi, max_phase, W, S, M, R, C, errbuf, errlen);
+  if (v != AMS_OK) return v;
+  if (!loss) { set_err(errbuf, errlen, "loss output is NULL"); return AMS_ERR_ARG; }
+  if (grad_phi && !H_a) { set_err(errbuf, errlen, "grad_phi needs a metasurface hop"); return AMS_ERR_ARG; }
+  const bool ms = H_a != nullptr;
+  ObjScratchLayout L = obj_scratch_layout(S, ms ? M : 0, R, C);
+  char *scr = nullptr;
+  CK(scratch_for(L.total, &scr));
+  ObjArgs a{H_d, H_a, H_r, phi, W, max_phase, S, ms ? M : 0, R, C, w, drop,
+            loss, grad_W, ms ? grad_phi : nullptr, recv_amp, grad_Y};
+  CK(obj_run(a, scr, (cudaStream_t)stream));
+  return AMS_OK;
+}
+
+ams_status ams_objective_recv(const float *H_d, const float *H_a, const float *H_r,
+                              const float *phi, float max_phase, const float *W, int S, int M,
+                              int R, int C, float *recv_amp, void *stream, char *errbuf,
+                              size_t errlen) {
+  ams_status v = obj_validate(H_d, H_a, H_r, phi, max_phase, W, S, M, R, C, errbuf, errlen);
+  if (v != AMS_OK) return v;
+  if (!recv_amp) { set_err(errbuf, errlen, "recv_amp is NULL"); return AMS_ERR_ARG; }
+  const bool ms = H_a != nullptr;
+  ObjScratchLayout L = obj_scratch_layout(S, ms ? M : 0, R, C);
+  char *scr = nullptr;
+  CK(scratch_for(L.total, &scr));
+  ObjArgs a{H_d, H_a, H_r, phi, W, max_phase, S, ms ? M : 0, R, C, 1.0f, nullptr,
+            nullptr, nullptr, nullptr, recv_amp, nullptr};
+  CK(obj_run(a, scr, (cudaStream_t)stream));
+  return AMS_OK;
+}
+
+ams_status ams_coverage_db(const float *H, int S, int R, float threshold, float offset, float *out,
+                           void *stream, char *errbuf, size_t errlen) {
+  if (!H || !out || S <= 0 || R <= 0) { set_err(errbuf, errlen, "bad arguments"); return AMS_ERR_ARG; }
+  CK(coverage_db_run(H, S, R, threshold, offset, out, (cudaStream_t)stream));
+  return AMS_OK;
+}
+
+unsigned long long ams_scratch_bytes(void) {
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  unsigned long long t = 0;
+  for (auto &d : g_scratch) t += d.cap;
+  return t;
+}
+
+}  // extern "C"

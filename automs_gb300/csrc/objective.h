@@ -1,0 +1,25 @@
+// objective.h -- launcher of the phase-map objective kernels (objective.cu).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+struct ObjArgs {
+  const float *Hd, *Ha, *Hr, *phi, *W;
+  float max_phase;
+  int S, M, R, C;
+  float w;
+  const uint8_t *drop;
+  float *loss, *grad_W, *grad_phi, *recv_amp, *grad_Y;
+};
+
+// byte offsets of the scratch regions for one problem size
+struct ObjScratchLayout {
+  size_t U, G1, G2, part, GU, inv, total;
+};
+
+ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C);
+// enqueue one evaluation on `st`; scratch must hold layout.total bytes
+cudaError_t obj_run(const ObjArgs &a, char *scratch, cudaStream_t st);
+cudaError_t coverage_db_run(const float *H, int S, int R, float threshold, float offset,
+                            float *out, cudaStream_t st);

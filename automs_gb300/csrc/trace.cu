@@ -1,0 +1,793 @@
+// trace.cu -- the two-stage ray-traced channel simulator on GB300.
+//
+// Reference behaviour (file:line of the reference):
+//   stage 1, forward discovery    optixPathTracer.cu:142-190, :285-331
+//   stage 2, backward verify      optixPathTracer.cu:191-273, :332-417
+//   sphere capture                optixPathTracer.cu:419-445
+//   beam patterns                 optixPathTracer.cu:107-136
+//   dedup + flood fill            optixPathTracer.cpp:127-354
+//
+// GB300 design:
+//   * software BVH traversal over LBVHs (lbvh.cu) with a per-thread stack;
+//     node culling is conservative, primitive tests are exact, and the
+//     closest hit is chosen by (t, instance, primitive), so the hit does not
+//     depend on traversal order.
+//   * stage 1 inserts each forward record straight into a hashed path table
+//     and a (cell x path) bitmap: no record buffer, no host round trip.
+//   * stage 2 works on bitmaps: a round is "list new tasks -> trace the
+//     25 x S backward rays of every task -> expand successes to the 4
+//     neighbour cells"; the host only reads the new-task count.
+//   * channel contributions are summed exactly in 64-bit fixed point, so H is
+//     bit-reproducible whatever the launch order.
+//   * this file is compiled with -fmad=false: the float arithmetic of every
+//     decision matches the CPU oracle bit for bit.
+#include "ams_common.cuh"
+#include "trace.h"
+
+namespace {
+
+// Largest floats not above cos((2k-1) pi / 72), k = 1..18: the 5-degree bin
+// edges of theta_id = int((acos|c| / (pi/2) * 36 + 1) / 2)
+// (optixPathTracer.cu:304-306).
+__constant__ unsigned c_theta_thr_bits[18] = {
+    0x3f7fc19fu, 0x3f7dcf54u, 0x3f79ee88u, 0x3f7426cbu, 0x3f6c835eu, 0x3f631324u,
+    0x3f57e880u, 0x3f4b1934u, 0x3f3cbe35u, 0x3f2cf37au, 0x3f1bd7c9u, 0x3f098c77u,
+    0x3eec6a50u, 0x3ec3ef15u, 0x3e99f61cu, 0x3e5da258u, 0x3e05a8a8u, 0x3d32aa3eu};
+
+__device__ __forceinline__ int theta_id(float c) {
+  float a = fabsf(c);
+  int id = 0;
+#pragma unroll
+  for (int k = 0; k < 18; k++) id += (a <= __uint_as_float(c_theta_thr_bits[k])) ? 1 : 0;
+  return id;
+}
+
+// ------------------------------------------------------------------- RNG
+// TEA-4 (Zafar, Olano, Curtis 2010) and the Numerical Recipes LCG
+// (optix/SDK/cuda/random.h:31-61)
+__device__ __forceinline__ uint32_t tea4(uint32_t v0, uint32_t v1) {
+  uint32_t s0 = 0;
+#pragma unroll
+  for (int n = 0; n < 4; n++) {
+    s0 += 0x9e3779b9u;
+    v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + s0) ^ ((v1 >> 5) + 0xc8013ea4u);
+    v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + s0) ^ ((v0 >> 5) + 0x7e95761eu);
+  }
+  return v0;
+}
+__device__ __forceinline__ float rnd(uint32_t &seed) {
+  seed = 1664525u * seed + 1013904223u;
+  return (float)(seed & 0x00FFFFFFu) / (float)0x01000000;
+}
+
+// sin/cos of a float angle in [0, 7): Cody-Waite reduction by pi/2 with a
+// two-part constant and Taylor series to degree 17/18 in double, rounded
+// once to float (correctly rounded except within ~1e-16 of a midpoint).
+__device__ __forceinline__ void sincos_exact(float a, float &s_out, float &c_out) {
+  double x = (double)a;
+  double kd = floor(x * 0.6366197723675814 + 0.5);
+  double r = (x - kd * 1.5707963267341256) - kd * 6.077100506506192e-11;
+  double r2 = r * r;
+  double s = 2.8114572543455206e-15;
+  s = s * r2 - 7.647163731819816e-13;
+  s = s * r2 + 1.6059043836821613e-10;
+  s = s * r2 - 2.505210838544172e-08;
+  s = s * r2 + 2.7557319223985893e-06;
+  s = s * r2 - 0.0001984126984126984;
+  s = s * r2 + 0.008333333333333333;
+  s = s * r2 - 0.16666666666666666;
+  s = s * r2 + 1.0;
+  s = s * r;
+  double c = 1.5619206968586225e-16;
+  c = c * r2 - 4.779477332387385e-14;
+  c = c * r2 + 1.1470745597729725e-11;
+  c = c * r2 - 2.08767569878681e-09;
+  c = c * r2 + 2.755731922398589e-07;
+  c = c * r2 - 2.48015873015873e-05;
+  c = c * r2 + 0.001388888888888889;
+  c = c * r2 - 0.041666666666666664;
+  c = c * r2 + 0.5;
+  c = 1.0 - c * r2;
+  int q = ((int)kd) & 3;
+  double so = q == 0 ? s : (q == 1 ? c : (q == 2 ? -s : -c));
+  double co = q == 0 ? c : (q == 1 ? -s : (q == 2 ? -c : s));
+  s_out = (float)so;
+  c_out = (float)co;
+}
+
+// rand_dir, optixPathTracer.cu:56-68
+__device__ __forceinline__ af3 rand_dir(uint32_t &seed, uint32_t ix, uint32_t iy, int lx, int ly) {
+  float rnd1 = (rnd(seed) + (float)ix) / (float)lx;
+  float rnd2 = (rnd(seed) + (float)iy) / (float)ly;
+  float theta = (2.0f * AMS_PIF) * rnd1;
+  float r = sqrtf(rnd2);
+  float sn, cs;
+  sincos_exact(theta, sn, cs);
+  float u = r * cs, v = r * sn;
+  float q = sqrtf(1.0f - r * r);
+  return mk3((2.0f * u) * q, (2.0f * v) * q, 1.0f - (2.0f * r) * r);
+}
+
+// get_beampattern_factor, optixPathTracer.cu:107-136; branches on the float
+// cosine against cos(120 deg) and cos(75 deg), taper value in float.
+__device__ __forceinline__ float beampattern(af3 d1, af3 d2, int type) {
+  float c = dot3(d1, d2) / (len3(d1) * len3(d2));
+  switch (type) {
+    case 0: return 1.0f;
+    case 1: return c < 0.0f ? 0.0f : c * 2.4495f;
+    case 2: {
+      if ((double)c < -0.5) return 0.1f;
+      if ((double)c < 0.25881904510252074) {
+        float th = acosf(c);
+        float e = (2.0943951f - th) * 0.31830987f * 4.0f * 0.41299623f - 1.0f;
+        return exp10f(e) * 2.4495f;
+      }
+      return (float)((double)c * 2.4495);
+    }
+    case 3: return c < 0.0f ? 0.0f : 1.4142f;
+    default: return 0.0f;
+  }
+}
+
+// ------------------------------------------------------------ primitives
+struct RayT {
+  af3 o, d, inv;
+  float oix, oiy, oiz;  // o * inv for the node test
+  int kx, ky, kz;
+  float Sx, Sy, Sz;
+};
+
+__device__ __forceinline__ void ray_setup(RayT &r, af3 o, af3 d) {
+  r.o = o;
+  r.d = d;
+  r.inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  r.oix = o.x * r.inv.x;
+  r.oiy = o.y * r.inv.y;
+  r.oiz = o.z * r.inv.z;
+  float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  int kz = (ax > ay) ? ((ax > az) ? 0 : 2) : ((ay > az) ? 1 : 2);
+  int kx = kz + 1; if (kx == 3) kx = 0;
+  int ky = kx + 1; if (ky == 3) ky = 0;
+  if (comp3(d, kz) < 0.0f) { int t = kx; kx = ky; ky = t; }
+  r.kx = kx; r.ky = ky; r.kz = kz;
+  float dz = comp3(d, kz);
+  r.Sx = comp3(d, kx) / dz;
+  r.Sy = comp3(d, ky) / dz;
+  r.Sz = 1.0f / dz;
+}
+
+// Watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2(1) 2013).
+__device__ __forceinline__ float tri_hit(const RayT &r, af3 v0, af3 v1, af3 v2) {
+  af3 A = sub3(v0, r.o), B = sub3(v1, r.o), C = sub3(v2, r.o);
+  float Az_ = comp3(A, r.kz), Bz_ = comp3(B, r.kz), Cz_ = comp3(C, r.kz);
+  float Ax = comp3(A, r.kx) - r.Sx * Az_;
+  float Ay = comp3(A, r.ky) - r.Sy * Az_;
+  float Bx = comp3(B, r.kx) - r.Sx * Bz_;
+  float By = comp3(B, r.ky) - r.Sy * Bz_;
+  float Cx = comp3(C, r.kx) - r.Sx * Cz_;
+  float Cy = comp3(C, r.ky) - r.Sy * Cz_;
+  float U = Cx * By - Cy * Bx;
+  float V = Ax * Cy - Ay * Cx;
+  float W = Bx * Ay - By * Ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return -1.0f;
+  float det = U + V + W;
+  if (det == 0.0f) return -1.0f;
+  float Az = r.Sz * Az_, Bz = r.Sz * Bz_, Cz = r.Sz * Cz_;
+  float T = U * Az + V * Bz + W * Cz;
+  return T / det;
+}
+
+// slab gate in front of the sphere program (AABB given by the caller)
+__device__ __forceinline__ bool prim_slab(const RayT &r, float4 lo, float4 hi) {
+  float tx0 = (lo.x - r.o.x) * r.inv.x, tx1 = (hi.x - r.o.x) * r.inv.x;
+  float ty0 = (lo.y - r.o.y) * r.inv.y, ty1 = (hi.y - r.o.y) * r.inv.y;
+  float tz0 = (lo.z - r.o.z) * r.inv.z, tz1 = (hi.z - r.o.z) * r.inv.z;
+  float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+  return tn <= tf && tf >= AMS_TMIN && tn <= AMS_TMAX;
+}
+
+// __intersection__sphere, optixPathTracer.cu:419-445; t = closest approach
+__device__ __forceinline__ float sphere_hit(const RayT &r, af3 center, float radius) {
+  af3 O = sub3(center, r.o);
+  af3 D = scl3(r.d, 1.0f / len3(r.d));
+  float b = dot3(O, D);
+  float c = dot3(O, O);
+  float acc = fmaxf(5e-5f, radius * radius);
+  if ((c - b * b < acc) && b > 0.0f && sqrtf(c) > radius) {
+    if (b > AMS_TMIN && b < AMS_TMAX) return b;
+  }
+  return -1.0f;
+}
+
+struct Hit { float t; int inst; int prim; };
+
+__device__ __forceinline__ bool better(float t, int inst, int prim, const Hit &h) {
+  if (t < h.t) return true;
+  if (t > h.t) return false;
+  if (inst != h.inst) return inst < h.inst;
+  return prim < h.prim;
+}
+
+// conservative child test: widened boxes, loosened far bound
+__device__ __forceinline__ bool child_test(const RayT &r, float lx, float ly, float lz, float hx,
+                                           float hy, float hz, float best, float &tn_out) {
+  float tx0 = __fmaf_rn(lx, r.inv.x, -r.oix), tx1 = __fmaf_rn(hx, r.inv.x, -r.oix);
+  float ty0 = __fmaf_rn(ly, r.inv.y, -r.oiy), ty1 = __fmaf_rn(hy, r.inv.y, -r.oiy);
+  float tz0 = __fmaf_rn(lz, r.inv.z, -r.oiz), tz1 = __fmaf_rn(hz, r.inv.z, -r.oiz);
+  float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+  tn_out = tn;
+  // the o*inv form loses a little accuracy; the slack below covers it
+  return tn <= __fmaf_rn(tf, 1.0001f, 1e-5f) && tf >= -1e-5f &&
+         tn <= __fmaf_rn(best, 1.0001f, 1e-4f);
+}
+
+template <int INST>
+__device__ __forceinline__ void test_prim(const float4 *prims, int j, const RayT &r, Hit &best,
+                                          float radius) {
+  const float4 a = __ldg(prims + 3 * j);
+  const float4 b = __ldg(prims + 3 * j + 1);
+  const float4 c = __ldg(prims + 3 * j + 2);
+  int orig = __float_as_int(a.w);
+  if (INST == 0) {
+    float t = tri_hit(r, mk3(a.x, a.y, a.z), mk3(b.x, b.y, b.z), mk3(c.x, c.y, c.z));
+    if (t > AMS_TMIN && t < AMS_TMAX && better(t, 0, orig, best)) {
+      best.t = t; best.inst = 0; best.prim = orig;
+    }
+  } else {
+    if (!prim_slab(r, b, c)) return;
+    float t = sphere_hit(r, mk3(a.x, a.y, a.z), radius);
+    if (t >= 0.0f && better(t, INST, orig, best)) {
+      best.t = t; best.inst = INST; best.prim = orig;
+    }
+  }
+}
+
+#define AMS_STACK 64
+#define AMS_SEG_CAP 65536  // closest-hit queries per ray before giving up
+
+template <int INST>
+__device__ void traverse(const BvhNode *nodes, const float4 *prims, int n, const RayT &r,
+                         Hit &best, float radius, unsigned *err) {
+  if (n <= 0) return;
+  if (n == 1) { test_prim<INST>(prims, 0, r, best, radius); return; }
+  int st_node[AMS_STACK];
+  float st_t[AMS_STACK];
+  int sp = 0;
+  int node = 0;
+  while (true) {
+    if ((unsigned)node >= (unsigned)(n - 1)) { atomicOr(err, AMS_DERR_BVH); return; }
+    const float4 *np = reinterpret_cast<const float4 *>(nodes + node);
+    const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+    const int4 d = __ldg(reinterpret_cast<const int4 *>(np + 3));
+    float tn0, tn1;
+    bool h0 = child_test(r, a.x, a.y, a.z, a.w, b.x, b.y, best.t, tn0);
+    bool h1 = child_test(r, b.z, b.w, c.x, c.y, c.z, c.w, best.t, tn1);
+    if (h0 && d.x < 0) {
+      if (~d.x >= n) { atomicOr(err, AMS_DERR_BVH); return; }
+      test_prim<INST>(prims, ~d.x, r, best, radius);
+      h0 = false;
+    }
+    if (h1 && d.y < 0) {
+      if (~d.y >= n) { atomicOr(err, AMS_DERR_BVH); return; }
+      test_prim<INST>(prims, ~d.y, r, best, radius);
+      h1 = false;
+    }
+    if (h0 && h1) {
+      int nearn = d.x, farn = d.y;
+      float tfar = tn1;
+      if (tn1 < tn0) { nearn = d.y; farn = d.x; tfar = tn0; }
+      if (sp < AMS_STACK) {
+        st_node[sp] = farn; st_t[sp] = tfar; sp++;
+      } else {
+        atomicOr(err, AMS_DERR_STACK);
+      }
+      node = nearn;
+    } else if (h0) {
+      node = d.x;
+    } else if (h1) {
+      node = d.y;
+    } else {
+      bool found = false;
+      while (sp > 0) {
+        sp--;
+        if (st_t[sp] <= __fmaf_rn(best.t, 1.0001f, 1e-4f)) { node = st_node[sp]; found = true; break; }
+      }
+      if (!found) break;
+    }
+  }
+}
+
+// optixTrace with a visibility mask: bit i selects instance i (0 scene,
+// 1 Tx spheres, 2 Rx spheres), optixPathTracer.cpp:417-424
+__device__ __forceinline__ Hit closest(const TraceDev &P, af3 o, af3 d, int mask) {
+  RayT r;
+  ray_setup(r, o, d);
+  Hit h;
+  h.t = AMS_TMAX; h.inst = 3; h.prim = 0x7fffffff;
+  if (mask & 1) traverse<0>(P.tri_nodes, P.tri_prims, P.n_tri, r, h, 0.0f, P.err);
+  if (mask & 2) traverse<1>(P.tx_nodes, P.tx_prims, P.n_src, r, h, P.src_r, P.err);
+  if (mask & 4) traverse<2>(P.rx_nodes, P.rx_prims, P.n_dst, r, h, P.dst_r, P.err);
+  return h;
+}
+
+// ---------------------------------------------------------- image method
+struct Mat34 { float m[12]; };
+
+__device__ __forceinline__ af3 image_of(const Mat34 &M, af3 p) {
+  const float *m = M.m;
+  return mk3(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3] * 1.0f,
+             m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7] * 1.0f,
+             m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11] * 1.0f);
+}
+
+// updateImageTransform, optixPathTracer.cu:70-76 (sum order of Matrix.h:339-356)
+__device__ __forceinline__ void image_update(Mat34 &M, af3 N, af3 A) {
+  float n[3] = {N.x, N.y, N.z};
+  float a[9];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      float p = (2.0f * n[i]) * n[j];
+      a[i * 3 + j] = (i == j ? 1.0f : 0.0f) - p;
+    }
+  Mat34 r;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      float s = a[i * 3] * M.m[j];
+      s = s + a[i * 3 + 1] * M.m[4 + j];
+      s = s + a[i * 3 + 2] * M.m[8 + j];
+      r.m[i * 4 + j] = s;
+    }
+  float k2 = 2.0f * dot3(A, N);
+  r.m[3] = r.m[3] + k2 * N.x;
+  r.m[7] = r.m[7] + k2 * N.y;
+  r.m[11] = r.m[11] + k2 * N.z;
+  M = r;
+}
+
+__device__ __forceinline__ int32_t fbits(float f) {
+  int32_t b = __float_as_int(f);
+  return b == (int32_t)0x80000000 ? 0 : b;  // -0 and +0 are one key
+}
+
+__device__ __forceinline__ uint64_t key_hash64(const int32_t *k) {
+  uint64_t h = 0x9E3779B97F4A7C15ull;
+#pragma unroll
+  for (int i = 0; i < 14; i++) h = mix64(h ^ ((uint64_t)(uint32_t)k[i] + ((uint64_t)i << 40)));
+  return h;
+}
+__device__ __forceinline__ uint32_t key_hash32(const int32_t *k) {
+  uint32_t h = 0x27d4eb2fu;
+#pragma unroll
+  for (int i = 0; i < 14; i++) h = mix32(h + 0x165667b1u * (uint32_t)(k[i] ^ (i * 0x61c88647)));
+  return h;
+}
+
+// claim or find the slot of a path key; returns -1 when the table is full
+__device__ int path_insert(const TraceDev &P, const int32_t *key) {
+  const uint64_t h = key_hash64(key) | 1ull;
+  const uint32_t c = key_hash32(key) | 1u;
+  uint32_t slot = (uint32_t)h & P.tab_mask;
+  for (uint32_t probe = 0; probe <= P.tab_mask; probe++) {
+    unsigned long long old = atomicCAS(P.tab_h + slot, 0ull, (unsigned long long)h);
+    if (old == 0ull) {
+      int32_t *dst = P.tab_key + (size_t)slot * 14;
+#pragma unroll
+      for (int i = 0; i < 14; i++) dst[i] = key[i];
+      unsigned o = atomicCAS(P.tab_chk + slot, 0u, c);
+      if (o != 0u && o != c) atomicOr(P.err, AMS_DERR_HASH);
+      unsigned long long occ = atomicAdd(P.ctr + 2, 1ull);
+      if (occ >= P.tab_limit) atomicOr(P.err, AMS_DERR_PATH_TABLE);
+      return (int)slot;
+    }
+    if (old == (unsigned long long)h) {
+      unsigned o = atomicCAS(P.tab_chk + slot, 0u, c);
+      if (o != 0u && o != c) atomicOr(P.err, AMS_DERR_HASH);
+      return (int)slot;
+    }
+    slot = (slot + 1u) & P.tab_mask;
+  }
+  atomicOr(P.err, AMS_DERR_PATH_TABLE);
+  return -1;
+}
+
+// scene triangle by original primitive index (optixPathTracer.cu:296-299)
+__device__ __forceinline__ void scene_tri(const TraceDev &P, int prim, af3 &v0, af3 &v1, af3 &v2) {
+  const float *v = P.tris + (size_t)prim * 9;
+  v0 = mk3(__ldg(v), __ldg(v + 1), __ldg(v + 2));
+  v1 = mk3(__ldg(v + 3), __ldg(v + 4), __ldg(v + 5));
+  v2 = mk3(__ldg(v + 6), __ldg(v + 7), __ldg(v + 8));
+}
+
+// ---------------------------------------------------------------- stage 1
+struct Slot {
+  af3 o, d;
+  Mat34 M;
+  int ttl;
+};
+
+
+
+__global__ void __launch_bounds__(128) k_stage1(TraceDev P) {
+  const long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long n_launch = (long long)P.launch_x * P.launch_y;
+  unsigned long long my_records = 0, my_segs = 0;
+  bool capped = false;
+  if (li < n_launch) {
+    const int ix = (int)(li / P.launch_y), iy = (int)(li % P.launch_y);
+    uint32_t seed = tea4((uint32_t)ix * (uint32_t)P.launch_y + (uint32_t)iy, 0u);
+    int res_cnt = 0;
+    int rec[AMS_MAX_RESERVE];  // cell * 8 + hit_cnt of the records kept so far
+    Slot slots[32];
+    const int L = P.L;
+    for (int launch = 0; launch < P.spl; launch++) {
+      float rs = rnd(seed) * (float)P.n_src;
+      uint32_t src = (uint32_t)rs;
+      if (src >= (uint32_t)P.n_src) src = (uint32_t)P.n_src - 1u;
+      const af3 spos = ld3(P.src + 3 * src);
+      slots[0].o = spos;
+      slots[0].d = rand_dir(seed, (uint32_t)ix, (uint32_t)iy, P.launch_x, P.launch_y);
+#pragma unroll
+      for (int k = 0; k < 12; k++) slots[0].M.m[k] = (k == 0 || k == 5 || k == 10) ? 1.0f : 0.0f;
+      slots[0].ttl = L + 1;
+      unsigned pending = 1u;
+      while (pending) {
+        const int i = __ffs(pending) - 1;
+        pending &= pending - 1u;
+        af3 o = slots[i].o, d = slots[i].d;
+        int ttl = slots[i].ttl;
+        int guard = 0;
+        while (ttl > 0) {
+          if (++guard > AMS_SEG_CAP) { atomicOr(P.err, AMS_DERR_LOOP); break; }
+          Hit h = closest(P, o, d, 5);
+          my_segs++;
+          if (h.inst == 3) break;
+          o = add3(o, scl3(d, h.t));
+          if (h.inst == 0 && ttl > 1) {
+            af3 v0, v1, v2;
+            scene_tri(P, h.prim, v0, v1, v2);
+            af3 N0 = nrm3(cross3(sub3(v1, v0), sub3(v2, v0)));
+            af3 N = faceforward3(N0, neg3(d), N0);
+            int m = __ldg(P.mat + h.prim);
+            float ct = dot3(d, N) / (len3(N) * len3(d));
+            int tid = theta_id(ct);
+            bool pen = __ldg(P.mat_prop + tid + m * AMS_NBINS) < 0.0f;
+            ttl--;
+            int hc = L + 1 - ttl;
+            int j = i | (1 << (hc - 1));
+            Slot &c = slots[j];
+            c.ttl = ttl;
+            c.o = o;
+            c.d = sub3(d, scl3(N, 2.0f * dot3(d, N)));
+            c.M = slots[i].M;
+            af3 V = sub3(v0, image_of(c.M, spos));
+            af3 Nimg = faceforward3(N0, V, N0);
+            image_update(c.M, Nimg, v0);
+            pending |= 1u << j;
+            if (!pen) ttl = 0;
+          } else if (h.inst == 2) {
+            if (res_cnt < P.reserve) {
+              int d0 = h.prim / P.n1_dst, d1 = h.prim % P.n1_dst;
+              int cell = (d0 / P.gs) * P.n1g + d1 / P.gs;
+              int hc = L + 1 - ttl;
+              int mhc = 0;
+              for (int k = res_cnt - 1; k >= 0; k--)
+                if ((rec[k] >> 3) == cell) { mhc = (rec[k] & 7) + 1; break; }
+              if (mhc <= hc) {
+                rec[res_cnt++] = cell * 8 + hc;
+                int32_t key[14];
+#pragma unroll
+                for (int k = 0; k < 12; k++) key[k] = fbits(slots[i].M.m[k]);
+                key[12] = hc;
+                key[13] = i;
+                int slot = path_insert(P, key);
+                if (slot >= 0)
+                  atomicOr(P.T + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
+                my_records++;
+              }
+            } else {
+              capped = true;
+            }
+          }
+        }
+      }
+    }
+  }
+  // block-aggregated counters
+  unsigned long long r = my_records, sg = my_segs;
+  for (int off = 16; off > 0; off >>= 1) {
+    r += __shfl_xor_sync(0xffffffffu, r, off);
+    sg += __shfl_xor_sync(0xffffffffu, sg, off);
+  }
+  unsigned cb = __ballot_sync(0xffffffffu, capped);
+  if ((threadIdx.x & 31) == 0) {
+    if (r) atomicAdd(P.ctr + 0, r);
+    if (sg) atomicAdd(P.ctr + 8, sg);
+    if (cb) atomicAdd(P.ctr + 1, (unsigned long long)__popc(cb));
+  }
+}
+
+// --------------------------------------------------------------- tasks
+// list the set bits of a [ng][W] bitmap as (cell, slot) tasks
+__global__ void k_make_tasks(TraceDev P, const unsigned *bits) {
+  const long long nwords = (long long)P.ng * P.W;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < nwords; base += stride) {
+    long long wi = base + threadIdx.x;
+    unsigned w = wi < nwords ? bits[wi] : 0u;
+    int cnt = __popc(w);
+    int incl = cnt;
+    for (int off = 1; off < 32; off <<= 1) {
+      int v = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += v;
+    }
+    int total = __shfl_sync(0xffffffffu, incl, 31);
+    unsigned long long start = 0;
+    if (lane == 31 && total) start = atomicAdd(P.ctr + 5, (unsigned long long)total);
+    start = __shfl_sync(0xffffffffu, start, 31);
+    if (!total) continue;
+    unsigned long long pos = start + (unsigned long long)(incl - cnt);
+    int cell = (int)(wi / P.W);
+    int wo = (int)(wi % P.W);
+    while (w) {
+      int b = __ffs(w) - 1;
+      w &= w - 1u;
+      if (pos < P.task_cap) P.tasks[pos] = make_int2(cell, wo * 32 + b);
+      else atomicOr(P.err, AMS_DERR_TASKS);
+      pos++;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- stage 2
+__global__ void __launch_bounds__(256) k_stage2(TraceDev P, unsigned long long n_tasks) {
+  const int S = P.n_src;
+  const int per_cell = P.gs * P.gs;
+  const unsigned long long per_task = (unsigned long long)per_cell * S;
+  const unsigned long long n_rays = n_tasks * per_task;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const float lam = P.lam_f;
+  const af3 srcdir = mk3(P.src_dir[0], P.src_dir[1], P.src_dir[2]);
+  const af3 dstdir = mk3(P.dst_dir[0], P.dst_dir[1], P.dst_dir[2]);
+  for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < n_rays;
+       base += stride) {
+    const unsigned long long ray = base + threadIdx.x;
+    bool valid = ray < n_rays;
+    long long task = -1;
+    bool ok = false, traced = false;
+    unsigned segs = 0;
+    int cell = 0, slot = 0, inner = 0, s = 0;
+    if (valid) {
+      task = (long long)(ray / per_task);
+      unsigned long long rem = ray % per_task;
+      inner = (int)(rem / S);
+      s = (int)(rem % S);
+      const int2 tk = P.tasks[task];
+      cell = tk.x;
+      slot = tk.y;
+      if ((unsigned)cell >= (unsigned)P.ng || (unsigned)slot > P.tab_mask) {
+        atomicOr(P.err, AMS_DERR_TASKS);
+        cell = 0;
+        slot = 0;
+        valid = false;
+      }
+    }
+    if (valid) {
+      const int gi = cell / P.n1g, gj = cell % P.n1g;
+      const int di = inner / P.gs + gi * P.gs, dj = inner % P.gs + gj * P.gs;
+      const int dst = di * P.n1_dst + dj;
+      bool skip = dst >= P.n_dst || (P.strict_grid && (di >= P.n0_dst || dj >= P.n1_dst));
+      if (!skip) {
+        traced = true;
+        const int32_t *key = P.tab_key + (size_t)slot * 14;
+        Mat34 M;
+#pragma unroll
+        for (int k = 0; k < 12; k++) M.m[k] = __int_as_float(__ldg(key + k));
+        const int hc = __ldg(key + 12), mask = __ldg(key + 13);
+        af3 o = ld3(P.dst + 3 * dst);
+        af3 d = nrm3(sub3(image_of(M, ld3(P.src + 3 * s)), o));
+        float amp = beampattern(d, dstdir, P.dst_bp);
+        float far = 1e6f, dd = 0.0f, dres = 0.0f;
+        double D = 0.0;
+        int ttl = hc + 1;
+        int guard = 0;
+        while (ttl > 0) {
+          if (++guard > AMS_SEG_CAP) { atomicOr(P.err, AMS_DERR_LOOP); break; }
+          Hit h = closest(P, o, d, 3);
+          segs++;
+          if (h.inst == 3) break;
+          const float t = h.t;
+          o = add3(o, scl3(d, t));
+          dd += t;
+          D += (double)t;
+          if (h.inst == 0) {
+            if (ttl == 1) break;
+            af3 v0, v1, v2;
+            scene_tri(P, h.prim, v0, v1, v2);
+            af3 N0 = nrm3(cross3(sub3(v1, v0), sub3(v2, v0)));
+            af3 N = faceforward3(N0, neg3(d), N0);
+            int m = __ldg(P.mat + h.prim);
+            float ct = dot3(d, N) / (len3(N) * len3(d));
+            float loss = fabsf(__ldg(P.mat_prop + theta_id(ct) + m * AMS_NBINS));
+            ttl--;
+            int hcb = hc + 1 - ttl;
+            int is_ref = (mask >> (hcb - 1)) & 1;
+            float max_d = fmaxf(fmaxf(len3(sub3(v0, v1)), len3(sub3(v1, v2))), len3(sub3(v2, v0)));
+            float fspl = 1.0f;
+            if (dd > far) { fspl = lam / ((4.0f * AMS_PIF) * dres); dres = 0.0f; }
+            amp *= loss * fspl;
+            dres += dd;
+            float fd = (float)(2.0 * (double)max_d * (double)max_d / (double)lam);
+            far = (dd > fd) ? fd : 1e6f;
+            dd = 0.0f;
+            if (is_ref) d = sub3(d, scl3(N, 2.0f * dot3(d, N)));
+          } else if (h.inst == 1 && h.prim == s) {
+            if (ttl == 1) {
+              float bp = beampattern(neg3(d), srcdir, P.src_bp);
+              float af = lam / ((4.0f * AMS_PIF) * (dres + dd));
+              amp *= bp * af;
+              ok = true;
+            }
+            break;
+          }
+        }
+        if (ok) {
+          // FP64 path length -> phase, reduced mod 2 pi in FP64
+          double ph = 6.283185307179586 * D / P.lam_d;
+          ph = ph - 6.283185307179586 * floor(ph / 6.283185307179586);
+          float sn, cs;
+          sincosf((float)ph, &sn, &cs);
+          double re = (double)(amp * cs), im = (double)(-amp * sn);
+          if (!(fabs(re) < AMS_ACC_LIMIT && fabs(im) < AMS_ACC_LIMIT)) {
+            atomicOr(P.err, AMS_DERR_ACC_RANGE);
+          } else {
+            unsigned long long *a = P.acc + ((size_t)s * P.n_dst + dst) * 2;
+            atomicAdd(a, (unsigned long long)__double2ll_rn(re * AMS_ACC_SCALE));
+            atomicAdd(a + 1, (unsigned long long)__double2ll_rn(im * AMS_ACC_SCALE));
+          }
+        }
+      }
+    }
+    // counters and the success bit of each task, one atomic per warp / task
+    unsigned okb = __ballot_sync(0xffffffffu, ok);
+    unsigned trb = __ballot_sync(0xffffffffu, traced);
+    for (int off = 16; off > 0; off >>= 1) segs += __shfl_xor_sync(0xffffffffu, segs, off);
+    if (lane == 0) {
+      if (segs) atomicAdd(P.ctr + 9, (unsigned long long)segs);
+      if (okb) atomicAdd(P.ctr + 3, (unsigned long long)__popc(okb));
+      if (trb & ~okb) atomicAdd(P.ctr + 4, (unsigned long long)__popc(trb & ~okb));
+    }
+    unsigned same = __match_any_sync(0xffffffffu, task);
+    unsigned any_ok = okb & same;
+    if (valid && any_ok && lane == __ffs(same) - 1)
+      atomicOr(P.S + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
+  }
+}
+
+// N = (S of the 4 neighbour cells) & ~T; T |= N; S = 0 (cpp:257-300).  The
+// neighbours are linear cell indices +-1 and +-n1g with only the [0, ng)
+// check, exactly as the reference (so row ends wrap).
+__global__ void k_expand(TraceDev P) {
+  const long long nwords = (long long)P.ng * P.W;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned long long cnt = 0;
+  for (long long wi = (long long)blockIdx.x * blockDim.x + threadIdx.x; wi < nwords; wi += stride) {
+    const int cell = (int)(wi / P.W);
+    const int w = (int)(wi % P.W);
+    unsigned s = 0;
+    const int nb[4] = {cell - 1, cell + 1, cell - P.n1g, cell + P.n1g};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (nb[k] >= 0 && nb[k] < P.ng) s |= P.S[(size_t)nb[k] * P.W + w];
+    unsigned t = P.T[wi];
+    unsigned n = s & ~t;
+    P.N[wi] = n;
+    if (n) P.T[wi] = t | n;
+    cnt += __popc(n);
+  }
+  for (int off = 16; off > 0; off >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(P.ctr + 7, cnt);
+}
+
+__global__ void k_clear(unsigned *p, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    p[i] = 0u;
+}
+
+__global__ void k_popcount(const unsigned *bits, long long n, unsigned long long *out) {
+  unsigned long long c = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    c += __popc(bits[i]);
+  for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(0xffffffffu, c, off);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+__global__ void k_finalize(const unsigned long long *acc, float *result, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long v = (long long)acc[i];
+    if (v) result[i] += (float)((double)v * AMS_ACC_INV);
+  }
+}
+
+__global__ void k_export(TraceDev P, int32_t *out, unsigned long long *n_out) {
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s <= P.tab_mask;
+       s += gridDim.x * blockDim.x) {
+    if (P.tab_h[s] == 0ull) continue;
+    unsigned long long k = atomicAdd(n_out, 1ull);
+    for (int i = 0; i < 14; i++) out[k * 14 + i] = P.tab_key[(size_t)s * 14 + i];
+  }
+}
+
+int grid_for(long long n, int block) {
+  long long b = (n + block - 1) / block;
+  const long long cap = 152LL * 16;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+}  // namespace
+
+cudaError_t trace_stage1(const TraceDev &P, cudaStream_t st) {
+  long long n = (long long)P.launch_x * P.launch_y;
+  int blocks = (int)((n + 127) / 128);
+  k_stage1<<<blocks, 128, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t trace_make_tasks(const TraceDev &P, const unsigned *bits, cudaStream_t st) {
+  long long n = (long long)P.ng * P.W;
+  k_make_tasks<<<grid_for(n, 256), 256, 0, st>>>(P, bits);
+  return cudaGetLastError();
+}
+
+cudaError_t trace_stage2(const TraceDev &P, unsigned long long n_tasks, cudaStream_t st) {
+  if (n_tasks == 0) return cudaSuccess;
+  unsigned long long rays = n_tasks * (unsigned long long)(P.gs * P.gs) * P.n_src;
+  long long blocks = (long long)((rays + 255) / 256);
+  const long long cap = 152LL * 8 * 16;
+  if (blocks > cap) blocks = cap;
+  k_stage2<<<(int)blocks, 256, 0, st>>>(P, n_tasks);
+  return cudaGetLastError();
+}
+
+cudaError_t trace_expand(const TraceDev &P, cudaStream_t st) {
+  long long n = (long long)P.ng * P.W;
+  k_expand<<<grid_for(n, 256), 256, 0, st>>>(P);
+  k_clear<<<grid_for(n, 256), 256, 0, st>>>(P.S, n);
+  return cudaGetLastError();
+}
+
+cudaError_t trace_count_bits(const TraceDev &P, const unsigned *bits, unsigned long long *out,
+                             cudaStream_t st) {
+  long long n = (long long)P.ng * P.W;
+  k_popcount<<<grid_for(n, 256), 256, 0, st>>>(bits, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t trace_finalize(const TraceDev &P, float *result, cudaStream_t st) {
+  long long n = (long long)P.n_src * P.n_dst * 2;
+  k_finalize<<<grid_for(n, 256), 256, 0, st>>>(P.acc, result, n);
+  return cudaGetLastError();
+}
+
+cudaError_t trace_export_paths(const TraceDev &P, int32_t *out, unsigned long long *n_out,
+                               cudaStream_t st) {
+  k_export<<<grid_for((long long)P.tab_mask + 1, 256), 256, 0, st>>>(P, out, n_out);
+  return cudaGetLastError();
+}

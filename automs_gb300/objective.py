@@ -1,0 +1,222 @@
+"""Phase-map objective: fused CUDA forward + adjoint behind autograd, and a
+Model / optimize_model pair with the interface of go.py:27-336.
+
+The objective and its hand-written adjoint run in libams.so
+(ams_objective_fwd_bwd); this module only wires them into
+torch.autograd.Function so that Adam (as in optimize_model, go.py:296-336)
+drives them.
+"""
+import ctypes as C
+import itertools
+import math
+import random
+
+import torch
+import torch.nn as nn
+
+from ._lib import call, lib
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _c64(t):
+    t = t.to(torch.complex64)
+    return t if t.is_contiguous() else t.contiguous()
+
+
+class CapacityObjective(torch.autograd.Function):
+    """loss(W, phi) of go.py:159-226 for one metasurface hop (or none):
+    Y = W H_d + ((W H_a) o e^{j (phi mod max_phase)}) H_r.
+    The adjoint is computed in the same call; backward only scales it."""
+
+    @staticmethod
+    def forward(ctx, W, phi, H_d, H_a, H_r, max_phase, w, drop, want_recv):
+        Cc, S = W.shape
+        R = H_d.shape[1]
+        ms = H_a is not None
+        M = H_a.shape[1] if ms else 0
+        Wc = _c64(W.detach())
+        Hd = _c64(H_d.detach())
+        Ha = _c64(H_a.detach()) if ms else None
+        Hr = _c64(H_r.detach()) if ms else None
+        ph = phi.detach().to(torch.float32).contiguous() if ms else None
+        loss = torch.empty((), dtype=torch.float32, device=W.device)
+        gW = torch.empty_like(Wc)
+        gphi = torch.empty(M, dtype=torch.float32, device=W.device) if ms else None
+        need_gy = H_d.requires_grad
+        gY = torch.empty(Cc, R, dtype=torch.complex64, device=W.device) if need_gy else None
+        recv = torch.empty(Cc, R, dtype=torch.float32, device=W.device) if want_recv else None
+        dr = drop.to(device=W.device, dtype=torch.uint8).contiguous() if drop is not None else None
+        call("ams_objective_fwd_bwd", _ptr(Hd), _ptr(Ha), _ptr(Hr), _ptr(ph), float(max_phase),
+             _ptr(Wc), S, M, R, Cc, float(w), _ptr(dr), _ptr(loss), _ptr(gW), _ptr(gphi),
+             _ptr(gY), _ptr(recv), _stream())
+        ctx.save_for_backward(gW, gphi if gphi is not None else torch.empty(0, device=W.device),
+                              gY if gY is not None else torch.empty(0, device=W.device), Wc)
+        ctx.ms = ms
+        ctx.need_gy = need_gy
+        ctx.w_dtype = W.dtype
+        if recv is not None:
+            ctx.mark_non_differentiable(recv)
+            return loss, recv
+        return loss, torch.empty(0, device=W.device)
+
+    @staticmethod
+    def backward(ctx, gl, _grecv):
+        gW, gphi, gY, Wc = ctx.saved_tensors
+        dW = (gW * gl).to(ctx.w_dtype) if ctx.needs_input_grad[0] else None
+        dphi = gphi * gl if (ctx.ms and ctx.needs_input_grad[1]) else None
+        dHd = None
+        if ctx.need_gy and ctx.needs_input_grad[2]:
+            # Y = W H_d  =>  dL/dH_d = W^H dL/dY (torch's complex convention)
+            dHd = (Wc.conj().transpose(0, 1) @ gY) * gl
+        return dW, dphi, dHd, None, None, None, None, None, None
+
+
+def capacity_objective(W, H_d, H_a=None, H_r=None, phi=None, max_phase=2 * math.pi, w=1.0,
+                       drop=None, return_recv=False):
+    """Differentiable objective.  W [C,S] complex, H_d [S,R], H_a [S,M],
+    H_r [M,R] complex64 CUDA tensors, phi [M] float, drop [C] bool."""
+    lib()
+    loss, recv = CapacityObjective.apply(W, phi, H_d, H_a, H_r, max_phase, w, drop, return_recv)
+    return (loss, recv) if return_recv else loss
+
+
+def mean_capacity(wvec, H_d, H_a=None, H_r=None, phi=None):
+    """-mean over Rx of log2(1 + |y|^2 / N0) with one complex weight vector:
+    the reference loss with C = 1, w = 1/R and no dropout."""
+    R = H_d.shape[1]
+    return capacity_objective(wvec.reshape(1, -1), H_d, H_a, H_r, phi, 2 * math.pi, 1.0 / R)
+
+
+class Model(nn.Module):
+    """go.py:27-245 with the objective on libams.so.
+
+    Same constructor, parameters (antenna_theta [C,S], ms_theta list),
+    attributes (loss_list, result, cap, max_code_ids) and loss.  The 10% code
+    dropout is drawn with torch.rand on the CPU generator as the reference
+    does (go.py:219-220); pass drop_rate=0 to disable it."""
+
+    def __init__(self, name, channels, ms_list, max_ms_reflex=2, code_num=60, w=1.0,
+                 global_random=False, drop_rate=0.1, device="cuda"):
+        super().__init__()
+        if isinstance(channels, dict):
+            channels = [channels]
+        self.name = name
+        self.ms_list = ms_list
+        self.max_ms_reflex = max_ms_reflex
+        self.channels = [{k: _c64(v.to(device)) for k, v in ch.items()} for ch in channels]
+        self.loss_list = []
+        self.w = w
+        self.global_random = global_random
+        self.drop_rate = drop_rate
+        S = self.channels[0]["src_to_dst"].shape[0]
+        A = torch.ones(code_num, S, dtype=torch.float32, device=device) / math.sqrt(S / 36)
+        if S == 36:
+            A[:, [0, 5, 30, 35]] = 0
+        self.antenna_A = A
+        self.antenna_theta = nn.Parameter(
+            torch.rand(code_num, S, dtype=torch.float32, device=device) * 2 * torch.pi)
+        self.ms_A = []
+        self.ms_theta = nn.ParameterList()
+        for i in range(len(ms_list)):
+            M = self.channels[0]["src_to_ms{%d}" % i].shape[1]
+            self.ms_A.append(torch.ones(M, dtype=torch.float32, device=device))
+            self.ms_theta.append(torch.zeros(M, dtype=torch.float32, device=device))
+        self.forward()
+
+    def postprocess(self):
+        """go.py:89-97: theta to pi/2 steps, phi into [0, max_phase)."""
+        self.antenna_theta = nn.Parameter(
+            torch.round(self.antenna_theta / (torch.pi / 2)) * (torch.pi / 2))
+        for i in range(len(self.ms_list)):
+            self.ms_theta[i] = self.ms_theta[i] % self.ms_list[i].max_phase
+        self.forward()
+
+    def pick_channel(self, choose_new=False):
+        if self.global_random:
+            if choose_new:
+                self.picked_channel = random.choice(self.channels)
+            return self.picked_channel
+        return random.choice(self.channels)
+
+    def _single_hop(self):
+        n = len(self.ms_list)
+        return n == 0 or self.max_ms_reflex == 0 or (n == 1 and self.max_ms_reflex >= 1)
+
+    def get_channel(self):
+        """Composite channel H [S, R] (go.py:107-157), in torch."""
+        channel = self.pick_channel(True)["src_to_dst"]
+        for L in range(1, self.max_ms_reflex + 1):
+            for path in itertools.product(range(len(self.ms_list)), repeat=L):
+                if any(path[i] == path[i + 1] for i in range(L - 1)):
+                    continue
+                msc = self.pick_channel()["src_to_ms{%d}" % path[0]]
+                for i, m in enumerate(path):
+                    real = self.ms_theta[m] % self.ms_list[m].max_phase
+                    msc = msc * (self.ms_A[m] * torch.exp(1j * real))
+                    if i == L - 1:
+                        msc = msc @ self.pick_channel()["ms{%d}_to_dst" % m]
+                    else:
+                        nx = path[i + 1]
+                        msc = msc @ (self.pick_channel()["ms{%d}_to_ms{%d}" % (m, nx)] if m < nx
+                                     else self.pick_channel()["ms{%d}_to_ms{%d}" % (nx, m)].T)
+                channel = channel + msc
+        return channel
+
+    def forward(self):
+        W = self.antenna_A * torch.exp(-1j * self.antenna_theta)
+        C_ = W.shape[0]
+        drop = torch.rand(C_) < self.drop_rate if self.drop_rate > 0 else None
+        if self._single_hop():
+            ch = self.pick_channel(True)
+            use_ms = len(self.ms_list) == 1 and self.max_ms_reflex >= 1
+            if use_ms:
+                loss, recv = capacity_objective(
+                    W, ch["src_to_dst"], ch["src_to_ms{0}"], ch["ms{0}_to_dst"], self.ms_theta[0],
+                    self.ms_list[0].max_phase, self.w, drop, return_recv=True)
+            else:
+                loss, recv = capacity_objective(W, ch["src_to_dst"], w=self.w, drop=drop,
+                                                return_recv=True)
+        else:
+            H = self.get_channel()
+            loss, recv = capacity_objective(W, H, w=self.w, drop=drop, return_recv=True)
+        self.result = recv.detach().clone()
+        self.max_code_ids = recv.max(0)[1].detach().clone()
+        eps = torch.finfo(torch.float32).eps
+        self.cap = torch.log2(1 + (recv + eps) ** 2 / 10 ** (-9)).detach()
+        self.loss = loss
+        return loss
+
+
+def optimize_model(model: Model, lr: float = 0.3, step: int = 200, progress=False):
+    """go.py:296-336: Adam over the model parameters, best-loss snapshot."""
+    opt = torch.optim.Adam(model.parameters(), lr=lr)
+    best = float("inf")
+    best_theta = None
+    best_ms = None
+    it = range(step)
+    if progress:
+        from tqdm import tqdm
+        it = tqdm(it)
+    for _ in it:
+        loss = model()
+        lv = loss.item()
+        if lv < best:
+            best = lv
+            best_theta = model.antenna_theta.detach().clone()
+            best_ms = [t.detach().clone() for t in model.ms_theta]
+        loss.backward()
+        opt.step()
+        opt.zero_grad()
+        model.loss_list.append(lv)
+    with torch.no_grad():
+        model.antenna_theta.copy_(best_theta)
+        for t, b in zip(model.ms_theta, best_ms):
+            t.copy_(b)
+    model.forward()

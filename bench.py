@@ -1,0 +1,360 @@
+"""Benchmark: ray-traced coverage (Rx-paths/s) on GB300.
+
+Headline workload "coverage-128": a 12 x 8 x 3 m room with 20 seeded
+floor-standing boxes (2172 triangles, reflection coefficients U[0.3, 0.7]),
+a 16-element half-wavelength ULA at 60 GHz, a 128 x 128 Rx grid at 1.5 m,
+a 1000 x 1000 forward launch and up to 2 reflections.  One step is one
+channel build (Tx/Rx BVH builds + stage 1 + all stage-2 rounds) on a scene
+whose triangle BVH is kept resident, as a user of the Scene API does.
+Rx-paths = successful backward verifications (the reference's stats[0]).
+
+Also reported: the plain phase-map objective (S=16, M=1024, R=4096, C=1)
+as objective+grad evals/s with its HBM roofline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "coverage Rx-paths/s"
+UNIT = "Rx-paths/s"
+WORKLOAD = ("coverage-128: 12x8x3 m room + 20 boxes (2172 tris), 16-el ULA @60 GHz, "
+            "128x128 Rx at 1.5 m, 1000x1000 launch, max_reflection=2")
+FLOP_PER_SEGMENT = 520  # closest-hit query on a ~2.1k-triangle scene (ideal leaf-4 BVH)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def kernel_launches(stats, aabbs_given):
+    """Kernels of one trace call: 2 sphere BVH builds (7 each, plus the AABB
+    kernel when the caller gives none), stage 1 + popcount, 4 per round,
+    the finalize pass."""
+    n = 14 + (0 if aabbs_given else 2) + 2 + 4 * stats["rounds"] + (1 if stats["fwd_records"] else 0)
+    return n
+
+
+def cpu_tracer_sample(cfg, threads):
+    import oracle
+    t0 = time.perf_counter()
+    _, st, _ = oracle.trace_channel(cfg["tris"], cfg["mat"], cfg["mat_prop"], cfg["src"],
+                                    cfg["dst"], cfg["params"], nthreads=threads)
+    dt = time.perf_counter() - t0
+    return st["rx_paths"], dt
+
+
+def run_reference(args, rank, world):
+    """The reference path's CPU restatement (oracle port, all host threads)."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from automs_gb300 import scenes
+    cfg = scenes.coverage_config("coverage-128", seed=0)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_tracer_sample(cfg, threads)
+    tot_p, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        p, t = cpu_tracer_sample(cfg, threads)
+        tot_p += p
+        tot_t += t
+    v = tot_p / tot_t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "one full coverage-128 build per step (C oracle, OpenMP)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def objective_bench(torch, steps, flush):
+    """Plain objective fwd+bwd, S=16 M=1024 R=4096 C=1, through the C ABI."""
+    import ctypes as C
+
+    from automs_gb300._lib import call
+    rng = np.random.Generator(np.random.PCG64(1))
+    S, M, R = 16, 1024, 4096
+    lam = 3e8 / 60e9
+
+    def cn(*sh):
+        d = rng.uniform(2.0, 15.0, size=sh)
+        g = (rng.normal(size=sh) + 1j * rng.normal(size=sh)) / np.sqrt(2)
+        return torch.as_tensor((g * lam / (4 * np.pi * d)).astype(np.complex64), device="cuda")
+    Hd, Ha, Hr = cn(S, R), cn(S, M), cn(M, R)
+    phi = torch.as_tensor(rng.uniform(0, 2 * np.pi, M).astype(np.float32), device="cuda")
+    wv = rng.normal(size=S) + 1j * rng.normal(size=S)
+    W = torch.as_tensor((wv / np.linalg.norm(wv)).astype(np.complex64)[None], device="cuda")
+    loss = torch.empty((), device="cuda")
+    gW = torch.empty_like(W)
+    gphi = torch.empty_like(phi)
+    P = lambda t: C.c_void_p(t.data_ptr())
+    st = torch.cuda.current_stream()
+
+    def once():
+        call("ams_objective_fwd_bwd", P(Hd), P(Ha), P(Hr), P(phi), float(2 * np.pi), P(W), S, M, R,
+             1, 1.0 / R, C.c_void_p(0), P(loss), P(gW), P(gphi), C.c_void_p(0), C.c_void_p(0),
+             C.c_void_p(st.cuda_stream))
+    for _ in range(5):
+        once()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        flush()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        once()
+        e1.record(st)
+        times.append((e0, e1))
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in times]
+    t = sum(ms) / len(ms)
+    bytes_alg = 8 * (R * M + M * S + R * S)
+    hbm, kind = peaks()
+    achieved = bytes_alg / (t * 1e-3) / 1e9
+    # host side: the same evaluation from host buffers (H2D of phi and w, D2H of loss + grads)
+    return {"metric": "objective+grad evals/s", "value": 1e3 / t, "unit": "evals/s",
+            "ms_per_eval": t, "config": {"S": S, "M": M, "R": R, "C": 1, "l2": "flushed"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None,
+                         "algorithmic_bytes": bytes_alg, "peak_kind": kind},
+            "gpu_launches_per_eval": 6}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from automs_gb300 import scenes, tracer
+
+    cfg = scenes.coverage_config("coverage-128", seed=rank)
+    scene = tracer.Scene(cfg["tris"], cfg["mat"], cfg["mat_prop"])
+    src = torch.as_tensor(cfg["src"], device="cuda")
+    dst = torch.as_tensor(cfg["dst"], device="cuda")
+    params = tracer.params_from_dict(cfg["params"])
+    S = src.shape[0] * src.shape[1]
+    Rn = dst.shape[0] * dst.shape[1]
+    result = torch.zeros(S, Rn, 2, device="cuda")
+    flushbuf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def flush():
+        flushbuf.fill_(1.0)
+
+    for _ in range(args.warmup):
+        result.zero_()
+        scene.trace(src, dst, params, result=result)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    steps = []
+    with ClockSampler(local) as clk:
+        barrier()
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            flush()
+            result.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _, st = scene.trace(src, dst, params, result=result)
+            e1.record(stream)
+            steps.append((e0, e1, st))
+        barrier()
+        t_wall = time.perf_counter() - t_wall
+    ms = [a.elapsed_time(b) for a, b, _ in steps]
+    total_ms = sum(ms)
+    paths = sum(s["rx_paths"] for _, _, s in steps)
+    st0 = steps[0][2]
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        p = torch.tensor([float(paths)], device="cuda")
+        dist.all_reduce(p, op=dist.ReduceOp.SUM)
+        total_ms, paths = float(t), float(p)
+    value = paths / (total_ms * 1e-3)
+
+    # ---- end to end through the public API from host buffers
+    h_tris = torch.as_tensor(cfg["tris"]).pin_memory()
+    h_mat = torch.as_tensor(cfg["mat"]).pin_memory()
+    h_mp = torch.as_tensor(cfg["mat_prop"]).pin_memory()
+    h_src = torch.as_tensor(cfg["src"]).pin_memory()
+    h_dst = torch.as_tensor(cfg["dst"]).pin_memory()
+    h_out = torch.empty(S, Rn, 2, dtype=torch.float32).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in (h_tris, h_mat, h_mp, h_src, h_dst))
+    d2h = h_out.numel() * 4
+    e2e_paths, e2e_t = 0, 0.0
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sc = tracer.Scene(h_tris.cuda(non_blocking=True), h_mat.cuda(non_blocking=True),
+                          h_mp.cuda(non_blocking=True))
+        res, st = sc.trace(h_src.cuda(non_blocking=True), h_dst.cuda(non_blocking=True), params)
+        h_out.copy_(res, non_blocking=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        sc.close()
+        if k >= args.warmup:
+            e2e_paths += st["rx_paths"]
+            e2e_t += dt
+    e2e = {"value": e2e_paths / e2e_t * world, "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h,
+           "note": "Scene creation (copies + triangle BVH) + trace + result download per step"}
+
+    obj = objective_bench(torch, 200, flush)
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    clocks = clk.summary()
+    hbm, peak_kind = peaks()
+    k2_ms = st0["ms_stage2_kernel"]
+    succ = st0["rx_paths"]
+    alg_bytes = 32 * succ + 64 * st0["tasks"]
+    achieved = alg_bytes / (k2_ms * 1e-3) / 1e9 if k2_ms > 0 else 0.0
+    sm_mhz = clocks["sm_mhz"] or 2070.0
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    flops = FLOP_PER_SEGMENT * st0["segments_bwd"]
+    tflops = flops / (k2_ms * 1e-3) / 1e12 if k2_ms > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            traffic = json.load(f).get("k_stage2_bytes_per_launch_coverage128")
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        threads = os.cpu_count() or 1
+        p_, t_ = cpu_tracer_sample(cfg, threads)
+        cpu = {"value": p_ / t_, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "one full coverage-128 build (C oracle, OpenMP)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 geometry, f64 phase",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "l2": "flushed between steps (256 MB write)",
+                   "rx_paths_per_step": st0["rx_paths"], "unique_paths": st0["unique_paths"],
+                   "rounds": st0["rounds"], "tasks": st0["tasks"],
+                   "ms_stage1": st0["ms_stage1"], "ms_stage2": st0["ms_stage2"],
+                   "ms_stage2_kernel": k2_ms, "ms_bvh": st0["ms_bvh"],
+                   "wall_s_timed_region": t_wall, "replicas": "one seeded scene per rank"},
+        "e2e": e2e,
+        "gpu_launches": kernel_launches(st0, False) * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "k_stage2", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
+                     "peak_kind": peak_kind,
+                     "note": "backward traversal is ALU/latency bound; see roofline_alu"},
+        "roofline_alu": {"bound": "fp32", "kernel": "k_stage2", "achieved": tflops,
+                         "peak": fp32_peak, "unit": "TFLOP/s", "frac": tflops / fp32_peak,
+                         "flop_per_segment": FLOP_PER_SEGMENT, "segments": st0["segments_bwd"],
+                         "peak_kind": "152 SM x 128 lanes x 2 at the sampled SM clock"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "secondary": [obj],
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+/*
+ * ams.h -- C ABI of the AutoMS GB300 library (libams.so).
+ *
+ * Plain pointers and sizes only.  Pointers documented "device" are CUDA
+ * device pointers (e.g. torch.Tensor.data_ptr() of a CUDA tensor); "host"
+ * pointers are ordinary host memory.  Every entry point returns an
+ * ams_status; on failure a message is written to errbuf (if given) and
+ * nothing is thrown across the ABI.  All work is enqueued on `stream`
+ * (a cudaStream_t, NULL = legacy default stream) and the call returns after
+ * the stream has finished the call's work, unless stated otherwise.
+ *
+ * Reference interfaces replaced (microsoft/AutoMS):
+ *   torch.ops.pathtrace.torch_launch_pathtrace   optixPathTracer.cpp:781-870
+ *   Model.get_channel / Model.forward / backward go.py:107-245
+ *   draw_channel coverage reduction             go.py:849-851, 944-964
+ */
+#ifndef AMS_H
+#define AMS_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int ams_status;
+#define AMS_OK 0
+#define AMS_ERR_ARG 1       /* bad argument (null pointer, size, type) */
+#define AMS_ERR_OOM 2       /* device allocation failed */
+#define AMS_ERR_CUDA 3      /* CUDA runtime / launch error */
+#define AMS_ERR_CAPACITY 4  /* a fixed capacity was exceeded */
+#define AMS_ERR_NUMERIC 6   /* value outside the representable range */
+#define AMS_ERR_INTERNAL 7  /* internal consistency check failed */
+
+/* Library version string. */
+const char *ams_version(void);
+
+/* ------------------------------------------------------------- tracer */
+
+/* Scene: triangles and materials, with the triangle BVH built once and kept
+ * across trace calls (the reference rebuilds its OptiX structures on every
+ * call, optixPathTracer.cpp:834-839).  One scene per host thread. */
+typedef struct ams_scene ams_scene;
+
+/* Launch parameters of one channel build; fields and meaning as the
+ * arguments of torch_launch_pathtrace (optixPathTracer.cpp:781-790). */
+typedef struct {
+  int samples_per_launch; /* rays per launch index */
+  int launch_x, launch_y; /* stage-1 launch grid */
+  double wave_len;        /* wavelength [m] */
+  int max_reflection;     /* 0..5 */
+  int reserve_size;       /* per-launch-index record cap, 1..256 */
+  int src_bptype, dst_bptype; /* beam pattern types 0..3 */
+  int dst_gridsize;       /* Rx cell edge (cells of gs x gs Rx) */
+  float src_r, dst_r;     /* sphere radii of Tx and Rx */
+  float src_dir[3], dst_dir[3]; /* array boresights (host values) */
+  int strict_grid;        /* 0 = reference behaviour at the grid edge */
+  int log_level;          /* 0 silent, 1 per-stage timings on stderr */
+} ams_trace_params;
+
+/* Counters of one build.  rx_paths is the reference's stats[0]
+ * (successful backward verifications), rx_fail its stats[1]. */
+typedef struct {
+  unsigned long long rx_paths, rx_fail;
+  unsigned long long fwd_records;    /* records kept by stage 1 */
+  unsigned long long unique_records; /* distinct (path, cell) pairs */
+  unsigned long long unique_paths;   /* distinct path keys */
+  unsigned long long rounds;         /* stage-2 rounds */
+  unsigned long long tasks;          /* (path, cell) tasks traced */
+  unsigned long long overflow;       /* launch indices that hit reserve_size */
+  float ms_bvh, ms_stage1, ms_stage2, ms_total;
+  unsigned long long workspace_bytes; /* device workspace high-water mark */
+  unsigned long long segments_fwd;   /* closest-hit queries of stage 1 */
+  unsigned long long segments_bwd;   /* closest-hit queries of stage 2 */
+  float ms_stage2_kernel;            /* device time of the backward kernels */
+} ams_stats;
+
+/* Create a scene from device arrays: tris [n_tri*9] float (3 vertices per
+ * triangle), mat [n_tri] int32 material ids, mat_prop [n_mat*19] float
+ * (angle-bin coefficients, negative = penetrable).  The arrays are copied.
+ * Replaces the scene part of optixPathTracer.cpp:382-546. */
+ams_status ams_scene_create(const float *tris, int n_tri, const int *mat,
+                            const float *mat_prop, int n_mat, void *stream,
+                            ams_scene **out, char *errbuf, size_t errlen);
+void ams_scene_destroy(ams_scene *scene);
+
+/* Build the channel from src [s0*s1*3] to dst [n0*n1*3] (device float) and
+ * ACCUMULATE it into result [s0*s1, n0*n1, 2] (device float, re/im
+ * interleaved), as the reference op does (optixPathTracer.cu:259-264).
+ * src_aabb/dst_aabb [n*6] (device) may be NULL: then pos -/+ r.
+ * stats may be NULL.  A build that finds no path is status AMS_OK with
+ * stats->unique_paths == 0 (the reference's "No path found!"). */
+ams_status ams_trace_channel(ams_scene *scene, const ams_trace_params *p,
+                             const float *src, int s0, int s1, const float *dst,
+                             int n0, int n1, const float *src_aabb,
+                             const float *dst_aabb, float *result,
+                             ams_stats *stats, void *stream, char *errbuf,
+                             size_t errlen);
+
+/* One-shot drop-in for torch_launch_pathtrace (optixPathTracer.cpp:781-790):
+ * same arguments in the same order, flattened to pointers and sizes.
+ * src_dir/dst_dir are HOST float[3] (the reference dereferences them on the
+ * host, optixPathTracer.cpp:827-828); every other array is device memory. */
+ams_status ams_launch_pathtrace(
+    float *result, const float *src, int s0, int s1, const float *dst, int n0,
+    int n1, const float *src_aabb, const float *dst_aabb,
+    const float *scene_tris, int n_tri, const int *mat,
+    int samples_per_launch, int launch_x, int launch_y, double wave_len,
+    int max_reflection, int reserve_size, const float *mat_prop, int n_mat,
+    const float *src_dir, const float *dst_dir, int log_level, int src_bptype,
+    int dst_bptype, int dst_gridsize, double src_r, double dst_r,
+    ams_stats *stats, char *errbuf, size_t errlen);
+
+/* Path list of the scene's last build: 14 int32 words per path (12 floats
+ * of the image transform, hit count, reflect mask; optixPathTracer.h:9-13),
+ * unordered, into host memory.  *n_out receives the number of paths. */
+ams_status ams_trace_export_paths(ams_scene *scene, int32_t *host_out,
+                                  int max_paths, int *n_out, char *errbuf,
+                                  size_t errlen);
+
+/* ----------------------------------------------------------- objective */
+
+/* Phase-map coverage objective and its adjoint (go.py:107-245, loss mode
+ * "capacity") for one metasurface hop:
+ *   Y = W H_d + ((W H_a) o exp(j (phi mod max_phase))) H_r     [C, R]
+ *   cap = log2(1 + (|Y| + eps)^2 / 1e-9)
+ *   cap' = cap with the rows where drop[c] != 0 zeroed
+ *   loss = -w * sum_r max_c cap' + || cap' o (cap' != max_c cap') ||_F
+ * All arrays are device memory, complex values are interleaved float pairs
+ * in the reference orientation: H_d [S,R], H_a [S,M], H_r [M,R], W [C,S].
+ * H_a/H_r/phi/grad_phi may be NULL (no metasurface, M ignored).  drop [C]
+ * uint8 may be NULL (no dropout).  Outputs: loss [1] float, grad_W [C,S]
+ * complex (dL/dRe + j dL/dIm), grad_phi [M] float, grad_Y [C,R] complex
+ * (gradient with respect to Y, for callers that compose the channel
+ * themselves), recv_amp [C,R] float (|Y|, Model.result of go.py:170); any of
+ * them may be NULL.  The call is asynchronous on `stream`.  Scratch memory is
+ * allocated internally on first use and kept across calls; calls on one
+ * device must not overlap. */
+ams_status ams_objective_fwd_bwd(const float *H_d, const float *H_a,
+                                 const float *H_r, const float *phi,
+                                 float max_phase, const float *W, int S, int M,
+                                 int R, int C, float w, const uint8_t *drop,
+                                 float *loss, float *grad_W, float *grad_phi,
+                                 float *grad_Y, float *recv_amp, void *stream,
+                                 char *errbuf, size_t errlen);
+
+/* Received amplitude |Y| [C,R] of the same model (forward only). */
+ams_status ams_objective_recv(const float *H_d, const float *H_a,
+                              const float *H_r, const float *phi,
+                              float max_phase, const float *W, int S, int M,
+                              int R, int C, float *recv_amp, void *stream,
+                              char *errbuf, size_t errlen);
+
+/* Coverage map in dB: 20 log10 |sum over Tx of H[:, r]| + offset, NaN or
+ * -inf replaced by threshold, clamped below at threshold
+ * (go.py:849-851, 944-964).  H [S,R] complex device, out [R] float device. */
+ams_status ams_coverage_db(const float *H, int S, int R, float threshold,
+                           float offset, float *out, void *stream,
+                           char *errbuf, size_t errlen);
+
+/* Device bytes held by the library's internal scratch (all objective calls
+ * on this device) -- for leak checks. */
+unsigned long long ams_scratch_bytes(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

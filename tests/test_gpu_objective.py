@@ -1,0 +1,134 @@
+"""CUDA objective + adjoint against the FP64 oracle and against the
+reference go.Model (golden fixtures)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import cases
+import objective_oracle as OO
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def obj():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from automs_gb300 import objective as O
+    return O
+
+
+def cuda(x):
+    return torch.as_tensor(x, device="cuda")
+
+
+@pytest.mark.parametrize("name", ["c1", "c30", "noms"])
+def test_fused_objective_vs_oracle(obj, name):
+    c = cases.objective_case(name)
+    ch = c["channels"]
+    A = OO.antenna_amplitude(c["code_num"], c["theta"].shape[1])
+    drop = np.zeros(c["code_num"], bool)
+    if c["code_num"] > 2:
+        drop[1] = True
+    mp = c["max_phase_deg"] / 180 * np.pi
+    Ha = ch.get("src_to_ms{0}") if c["n_ms"] else None
+    Hr = ch.get("ms{0}_to_dst") if c["n_ms"] else None
+    phi = c["phi"][0] if c["n_ms"] else None
+    loss_o, gth_o, gphi_o, ex = OO.objective(ch["src_to_dst"], Ha, Hr, phi, c["theta"], A, c["w"],
+                                             drop, mp)
+    theta = cuda(c["theta"]).requires_grad_(True)
+    W = cuda(A.astype(np.float32)) * torch.exp(-1j * theta)
+    ph = cuda(phi).requires_grad_(True) if phi is not None else None
+    loss, recv = obj.capacity_objective(W, cuda(ch["src_to_dst"]), cuda(Ha) if Ha is not None else None,
+                                        cuda(Hr) if Hr is not None else None, ph, mp, c["w"],
+                                        cuda(drop), return_recv=True)
+    loss.backward()
+    np.testing.assert_allclose(float(loss), loss_o, rtol=1e-4)
+    np.testing.assert_allclose(recv.cpu().numpy(), ex["amp"], rtol=1e-4, atol=1e-9)
+    g = theta.grad.cpu().numpy()
+    np.testing.assert_allclose(g, gth_o, rtol=1e-3, atol=1e-3 * np.abs(gth_o).max())
+    if ph is not None:
+        gp = ph.grad.cpu().numpy()
+        np.testing.assert_allclose(gp, gphi_o, rtol=1e-3, atol=1e-3 * np.abs(gphi_o).max())
+
+
+@pytest.mark.parametrize("name", cases.OBJECTIVE_CASES)
+def test_model_matches_reference_model(obj, name):
+    """automs_gb300.objective.Model against go.Model run by the reference
+    (same inputs, same dropout rows)."""
+    from automs_gb300.geometry import Metasurface
+    g = np.load(os.path.join(GOLD, f"obj_{name}.npz"))
+    c = cases.objective_case(name)
+    chans = {k: cuda(v) for k, v in c["channels"].items()}
+    ms = [Metasurface(None, None, None, None, None, c["max_phase_deg"]) for _ in range(c["n_ms"])]
+    m = obj.Model(name, chans, ms, max_ms_reflex=c["max_ms_reflex"], code_num=c["code_num"],
+                  w=c["w"], drop_rate=0.0)
+    with torch.no_grad():
+        m.antenna_theta.copy_(cuda(c["theta"]))
+        for i in range(c["n_ms"]):
+            m.ms_theta[i].copy_(cuda(c["phi"][i]))
+    m.drop_rate = 0.0
+    W = m.antenna_A * torch.exp(-1j * m.antenna_theta)
+    if m._single_hop():
+        ch = m.channels[0]
+        args = (ch["src_to_ms{0}"], ch["ms{0}_to_dst"], m.ms_theta[0], ms[0].max_phase) \
+            if c["n_ms"] else (None, None, None, 2 * np.pi)
+        loss = obj.capacity_objective(W, ch["src_to_dst"], args[0], args[1], args[2], args[3],
+                                      c["w"], cuda(g["drop"]))
+    else:
+        loss = obj.capacity_objective(W, m.get_channel(), w=c["w"], drop=cuda(g["drop"]))
+    loss.backward()
+    np.testing.assert_allclose(float(loss), float(g["loss"]), rtol=2e-4)
+    gt = g["grad_theta"]
+    np.testing.assert_allclose(m.antenna_theta.grad.cpu().numpy(), gt, rtol=5e-3,
+                               atol=5e-3 * np.abs(gt).max())
+    for i in range(c["n_ms"]):
+        gp = g[f"grad_phi{i}"]
+        np.testing.assert_allclose(m.ms_theta[i].grad.cpu().numpy(), gp, rtol=5e-3,
+                                   atol=5e-3 * np.abs(gp).max())
+
+
+def test_objective_config_size(obj):
+    """The S=16, M=1024, R=4096 plain objective (C=1) against the oracle."""
+    rng = np.random.Generator(np.random.PCG64(11))
+    S, M, R = 16, 1024, 4096
+    Hd = cases._cn(rng, (S, R))
+    Ha = cases._cn(rng, (S, M))
+    Hr = cases._cn(rng, (M, R))
+    phi = rng.uniform(0, 2 * np.pi, M).astype(np.float32)
+    wv = (rng.normal(size=S) + 1j * rng.normal(size=S)).astype(np.complex64)
+    wv /= np.linalg.norm(wv)
+    loss_o, gW_o, gphi_o = OO.mean_capacity(Hd, Ha, Hr, phi, wv)
+    w = cuda(wv).requires_grad_(True)
+    p = cuda(phi).requires_grad_(True)
+    loss = obj.mean_capacity(w, cuda(Hd), cuda(Ha), cuda(Hr), p)
+    loss.backward()
+    np.testing.assert_allclose(float(loss), loss_o, rtol=1e-5)
+    np.testing.assert_allclose(w.grad.cpu().numpy(), gW_o, rtol=1e-3, atol=1e-3 * np.abs(gW_o).max())
+    np.testing.assert_allclose(p.grad.cpu().numpy(), gphi_o, rtol=1e-3,
+                               atol=1e-3 * np.abs(gphi_o).max())
+
+
+def test_optimize_model_decreases_loss(obj):
+    from automs_gb300.geometry import Metasurface
+    c = cases.objective_case("c30")
+    chans = {k: cuda(v) for k, v in c["channels"].items()}
+    torch.manual_seed(0)
+    m = obj.Model("t", chans, [Metasurface(None, None, None, None, None, 300)], max_ms_reflex=1,
+                  code_num=30, w=0.5)
+    obj.optimize_model(m, step=30)
+    assert m.loss_list[-1] < m.loss_list[0]
+
+
+def test_coverage_db(obj):
+    from automs_gb300 import tracer
+    rng = np.random.Generator(np.random.PCG64(5))
+    H = (rng.normal(size=(4, 300)) + 1j * rng.normal(size=(4, 300))).astype(np.complex64) * 1e-3
+    H[:, 7] = 0
+    out = tracer.coverage_db(cuda(H), threshold=-150.0).cpu().numpy()
+    ref = 20 * np.log10(np.abs(H.sum(0).astype(np.complex128)))
+    ref = np.maximum(np.where(np.isnan(ref), -150.0, ref), -150.0)
+    np.testing.assert_allclose(out, ref, atol=1e-4)

@@ -1,0 +1,139 @@
+"""CUDA tracer against the oracle (bit-exact ray sets) and against the
+reference's own device programs (golden fixtures)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import cases
+import oracle
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def tracer():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from automs_gb300 import tracer as T
+    return T
+
+
+def run_gpu(T, c):
+    sc = T.Scene(c["tris"], c["mat"], c["mat_prop"])
+    res, st = sc.trace(c["src"], c["dst"], c["params"])
+    torch.cuda.synchronize()
+    paths = sc.export_paths()
+    sc.close()
+    H = (res[..., 0] + 1j * res[..., 1]).cpu().numpy()
+    return H, st, paths
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+
+@pytest.mark.parametrize("name", cases.CHANNEL_CASES)
+def test_channel_parity_with_oracle(tracer, name):
+    c = cases.channel_case(name)
+    H, st, paths = run_gpu(tracer, c)
+    Ho, so, po = oracle.trace_channel(c["tris"], c["mat"], c["mat_prop"], c["src"], c["dst"],
+                                      c["params"])
+    for k in cases.STAT_KEYS + ("tasks", "overflow"):
+        assert st[k] == so[k], (k, st[k], so[k])
+    assert np.array_equal(paths, po)
+    # same ray set; the phase is FP64 on both sides, sin/cos differ in the last bits
+    assert np.array_equal(H != 0, Ho != 0)
+    assert rel(H, Ho) < 1e-5
+    g = np.load(os.path.join(GOLD, f"chan_{name}.npz"))
+    assert [st[k] for k in cases.STAT_KEYS] == list(g["stats"])
+    assert np.array_equal(paths, g["paths"])
+    pw, pr = np.abs(H.sum(0)) ** 2, np.abs(g["H"].sum(0)) ** 2
+    m = pr > 0
+    assert np.abs(10 * np.log10(pw[m] / pr[m])).max() < 0.1
+
+
+def test_deterministic_and_accumulating(tracer):
+    c = cases.channel_case("small")
+    sc = tracer.Scene(c["tris"], c["mat"], c["mat_prop"])
+    r1, s1 = sc.trace(c["src"], c["dst"], c["params"])
+    r2, s2 = sc.trace(c["src"], c["dst"], c["params"])
+    assert torch.equal(r1, r2) and s1["rx_paths"] == s2["rx_paths"]
+    base = torch.full_like(r1, 0.25)
+    r3, _ = sc.trace(c["src"], c["dst"], c["params"], result=base.clone())
+    assert torch.allclose(r3, r1 + 0.25, rtol=0, atol=1e-6)
+    sc.close()
+
+
+def test_strict_grid_drops_wrapped_rx(tracer):
+    c = cases.channel_case("tiny")
+    c["params"]["strict_grid"] = 1
+    H, st, _ = run_gpu(tracer, c)
+    Ho, so, _ = oracle.trace_channel(c["tris"], c["mat"], c["mat_prop"], c["src"], c["dst"],
+                                     c["params"])
+    assert st["rx_paths"] == so["rx_paths"]
+    assert rel(H, Ho) < 1e-5
+
+
+def test_mid_size_parity(tracer):
+    """A 48x48 Rx grid with a 256x256 launch: still exact against the oracle."""
+    from automs_gb300 import scenes
+    c = scenes.coverage_config("coverage-small")
+    c["dst"] = scenes.rx_grid(0.25, 11.75, 48, 0.25, 7.75, 48, 1.5)
+    c["params"]["launch_x"] = c["params"]["launch_y"] = 256
+    H, st, paths = run_gpu(tracer, c)
+    Ho, so, po = oracle.trace_channel(c["tris"], c["mat"], c["mat_prop"], c["src"], c["dst"],
+                                      c["params"])
+    assert st["rx_paths"] == so["rx_paths"] and st["unique_records"] == so["unique_records"]
+    assert np.array_equal(paths, po)
+    assert rel(H, Ho) < 1e-5
+
+
+def test_full_coverage_config_properties(tracer):
+    """The 128x128 / 1M-ray coverage workload: deterministic, finite, with
+    per-Rx power inside physical bounds."""
+    from automs_gb300 import scenes
+    c = scenes.coverage_config("coverage-128")
+    sc = tracer.Scene(c["tris"], c["mat"], c["mat_prop"])
+    r1, s1 = sc.trace(c["src"], c["dst"], c["params"])
+    r2, s2 = sc.trace(c["src"], c["dst"], c["params"])
+    sc.close()
+    assert torch.equal(r1, r2)
+    assert s1["rx_paths"] > 1_000_000 and s1["overflow"] == 0
+    H = torch.complex(r1[..., 0], r1[..., 1])
+    db = tracer.coverage_db(H)
+    assert torch.isfinite(db).all()
+    assert float(db.max()) < 0.0  # no gain above free space at these distances
+
+
+def test_launch_pathtrace_dropin(tracer):
+    c = cases.channel_case("tiny")
+    p = c["params"]
+    src = torch.as_tensor(c["src"], device="cuda")
+    dst = torch.as_tensor(c["dst"], device="cuda")
+    res = torch.zeros(src.shape[0] * src.shape[1], dst.shape[0] * dst.shape[1], 2, device="cuda")
+    st = tracer.launch_pathtrace(
+        res, src, dst, torch.cat([src - p["src_r"], src + p["src_r"]], -1),
+        torch.cat([dst - p["dst_r"], dst + p["dst_r"]], -1),
+        torch.as_tensor(c["tris"], device="cuda").reshape(-1, 3),
+        torch.as_tensor(c["mat"], device="cuda"), 1, p["launch_x"], p["launch_y"], p["wave_len"],
+        p["max_reflection"], p["reserve_size"], torch.as_tensor(c["mat_prop"], device="cuda"),
+        torch.tensor(p["src_dir"]), torch.tensor(p["dst_dir"]), 0, p["src_bptype"],
+        p["dst_bptype"], p["dst_gridsize"], p["src_r"], p["dst_r"])
+    g = np.load(os.path.join(GOLD, "chan_tiny.npz"))
+    assert st["rx_paths"] == int(g["stats"][0])
+
+
+def test_errors_raise(tracer):
+    from automs_gb300._lib import AmsError
+    c = cases.channel_case("tiny")
+    sc = tracer.Scene(c["tris"], c["mat"], c["mat_prop"])
+    bad = dict(c["params"], max_reflection=6)
+    with pytest.raises(AmsError):
+        sc.trace(c["src"], c["dst"], bad)
+    # the scene still works after a rejected call
+    _, st = sc.trace(c["src"], c["dst"], c["params"])
+    assert st["rx_paths"] > 0
+    sc.close()
