@@ -203,6 +203,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", default="all", choices=["all", "tracer", "objective"],
+                    help="profiling aid: run only the named timed loop")
+    ap.add_argument("--launch", type=int, default=0,
+                    help="profiling aid: override the forward launch edge (default 1000)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -221,6 +225,12 @@ def main():
     from automs_gb300 import scenes, tracer
 
     cfg = scenes.coverage_config("coverage-128", seed=rank)
+    if args.launch:
+        cfg["params"]["launch_x"] = cfg["params"]["launch_y"] = args.launch
+    if args.only == "objective":
+        flushbuf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        print(json.dumps(objective_bench(torch, args.steps, lambda: flushbuf.fill_(1.0))))
+        return
     scene = tracer.Scene(cfg["tris"], cfg["mat"], cfg["mat_prop"])
     src = torch.as_tensor(cfg["src"], device="cuda")
     dst = torch.as_tensor(cfg["dst"], device="cuda")
@@ -270,6 +280,10 @@ def main():
         dist.all_reduce(p, op=dist.ReduceOp.SUM)
         total_ms, paths = float(t), float(p)
     value = paths / (total_ms * 1e-3)
+    if args.only == "tracer":
+        print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": total_ms / args.steps,
+                          "stats": {k: v for k, v in steps[0][2].items()}}))
+        return
 
     # ---- end to end through the public API from host buffers
     h_tris = torch.as_tensor(cfg["tris"]).pin_memory()
