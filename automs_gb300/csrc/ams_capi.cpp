@@ -497,6 +497,8 @@ cudaError_t scratch_for(size_t bytes, char **out) {
     }
     size_t want = std::max(bytes, (size_t)1 << 20);
     if ((e = cudaMalloc(&d.ptr, want)) != cudaSuccess) return e;
+    // the control block (arrival counter) must start at zero
+    if ((e = cudaMemset(d.ptr, 0, kObjControlBytes)) != cudaSuccess) return e;
     d.cap = want;
   }
   *out = d.ptr;

@@ -55,269 +55,291 @@ __device__ __forceinline__ float py_mod(float a, float b) {
   return r;
 }
 
-// U[c,m] = sum_s W[c,s] H_a[s,m] * exp(j phi'_m)
-__global__ void k_prep(const float *W, const float *Ha, const float *phi, float max_phase, int S,
-                       int M, int C, float *U) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
-  int c = blockIdx.y;
-  if (m >= M) return;
+// ------------------------------------------------------------------
+// Virtual rows k in [0, K), K = M + S: row k < M is H_r[k, :] with
+// coefficient U[c, k]; row k >= M is H_d[k - M, :] with coefficient
+// W[c, k - M].  Y[c, r] = sum_k coef[c, k] row_k[r].
+
+__device__ __forceinline__ c2 coef_u(const float *W, const float *Ha, const float *phi,
+                                     float max_phase, int S, int M, int c, int m) {
   c2 v = {0.f, 0.f};
   for (int s = 0; s < S; s++) mac(v, ld2(W, (size_t)c * S + s), ld2(Ha, (size_t)s * M + m));
-  float p = py_mod(phi[m], max_phase);  // go.py:133
+  float p = py_mod(__ldg(phi + m), max_phase);  // go.py:133
   float sn, cs;
   sincosf(p, &sn, &cs);
-  c2 e = {cs, sn};
   c2 u = {0.f, 0.f};
-  mac(u, v, e);
-  reinterpret_cast<float2 *>(U)[(size_t)c * M + m] = make_float2(u.x, u.y);
+  mac(u, v, c2{cs, sn});
+  return u;
 }
 
-// Y over one r per thread, all codes in registers; then the per-Rx loss
-// terms and gradient parts.
+__device__ __forceinline__ const float *row_ptr(const float *Hr, const float *Hd, int M, int R,
+                                                int k) {
+  return k < M ? Hr + (size_t)k * R * 2 : Hd + (size_t)(k - M) * R * 2;
+}
+
+constexpr int KCHUNK = 256;
+
+// pass 1: partial Y over a k-range; lanes = 32 columns, warps share the rows
 template <int CB>
-__global__ void __launch_bounds__(128) k_pass1(const float *Hd, const float *W, const float *Hr,
-                                               const float *U, int S, int M, int R, int C, float w,
-                                               const uint8_t *drop, float *G1, float *G2,
-                                               double *partials, float *recv_amp) {
-  __shared__ c2 sU[64][CB];
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = r < R;
+__global__ void __launch_bounds__(256) k_pass1(ObjArgs a, int M, int K, int kper, float *Ypart) {
+  __shared__ c2 sC[KCHUNK][CB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int r = blockIdx.x * 32 + lane;
+  const bool live = r < a.R;
+  const int k0 = blockIdx.y * kper, k1 = min(K, k0 + kper);
   c2 y[CB];
 #pragma unroll
   for (int c = 0; c < CB; c++) y[c] = {0.f, 0.f};
-  // W H_d
-  for (int k0 = 0; k0 < S; k0 += 64) {
-    int kn = min(64, S - k0);
+  for (int kc = k0; kc < k1; kc += KCHUNK) {
+    const int kn = min(KCHUNK, k1 - kc);
     __syncthreads();
     for (int i = threadIdx.x; i < kn * CB; i += blockDim.x) {
-      int k = i / CB, c = i % CB;
-      sU[k][c] = c < C ? ld2(W, (size_t)c * S + k0 + k) : c2{0.f, 0.f};
+      const int kk = i / CB, c = i % CB, k = kc + kk;
+      c2 v = {0.f, 0.f};
+      if (c < a.C) v = k < M ? coef_u(a.W, a.Ha, a.phi, a.max_phase, a.S, M, c, k)
+                             : ld2(a.W, (size_t)c * a.S + (k - M));
+      sC[kk][c] = v;
     }
     __syncthreads();
-    if (live)
-      for (int k = 0; k < kn; k++) {
-        c2 h = ld2(Hd, (size_t)(k0 + k) * R + r);
+    if (live) {
+      int kk = warp;
+      for (; kk + 24 < kn; kk += 32) {
+        const c2 h0 = ld2(row_ptr(a.Hr, a.Hd, M, a.R, kc + kk), r);
+        const c2 h1 = ld2(row_ptr(a.Hr, a.Hd, M, a.R, kc + kk + 8), r);
+        const c2 h2 = ld2(row_ptr(a.Hr, a.Hd, M, a.R, kc + kk + 16), r);
+        const c2 h3 = ld2(row_ptr(a.Hr, a.Hd, M, a.R, kc + kk + 24), r);
 #pragma unroll
-        for (int c = 0; c < CB; c++) mac(y[c], sU[k][c], h);
-      }
-  }
-  // U H_r
-  if (Hr) {
-    for (int k0 = 0; k0 < M; k0 += 64) {
-      int kn = min(64, M - k0);
-      __syncthreads();
-      for (int i = threadIdx.x; i < kn * CB; i += blockDim.x) {
-        int k = i / CB, c = i % CB;
-        sU[k][c] = c < C ? ld2(U, (size_t)c * M + k0 + k) : c2{0.f, 0.f};
-      }
-      __syncthreads();
-      if (live) {
-        int k = 0;
-        for (; k + 4 <= kn; k += 4) {
-          c2 h0 = ld2(Hr, (size_t)(k0 + k) * R + r), h1 = ld2(Hr, (size_t)(k0 + k + 1) * R + r);
-          c2 h2 = ld2(Hr, (size_t)(k0 + k + 2) * R + r), h3 = ld2(Hr, (size_t)(k0 + k + 3) * R + r);
-#pragma unroll
-          for (int c = 0; c < CB; c++) {
-            mac(y[c], sU[k][c], h0);
-            mac(y[c], sU[k + 1][c], h1);
-            mac(y[c], sU[k + 2][c], h2);
-            mac(y[c], sU[k + 3][c], h3);
-          }
+        for (int c = 0; c < CB; c++) {
+          mac(y[c], sC[kk][c], h0);
+          mac(y[c], sC[kk + 8][c], h1);
+          mac(y[c], sC[kk + 16][c], h2);
+          mac(y[c], sC[kk + 24][c], h3);
         }
-        for (; k < kn; k++) {
-          c2 h = ld2(Hr, (size_t)(k0 + k) * R + r);
+      }
+      for (; kk < kn; kk += 8) {
+        const c2 h = ld2(row_ptr(a.Hr, a.Hd, M, a.R, kc + kk), r);
 #pragma unroll
-          for (int c = 0; c < CB; c++) mac(y[c], sU[k][c], h);
-        }
+        for (int c = 0; c < CB; c++) mac(y[c], sC[kk][c], h);
       }
     }
   }
+  // reduce the 8 warps, 8 codes at a time
+  __shared__ c2 red[8][32][8];
+  for (int cg = 0; cg < CB; cg += 8) {
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      if (cg + j < CB) red[warp][lane][j] = y[cg + j < CB ? cg + j : 0];
+    __syncthreads();
+    if (warp == 0 && live) {
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int c = cg + j;
+        if (c >= CB || c >= a.C) continue;
+        c2 t = red[0][lane][j];
+        for (int w2 = 1; w2 < 8; w2++) { t.x += red[w2][lane][j].x; t.y += red[w2][lane][j].y; }
+        reinterpret_cast<float2 *>(Ypart)[((size_t)blockIdx.y * a.C + c) * a.R + r] =
+            make_float2(t.x, t.y);
+      }
+    }
+  }
+}
+
+// epilogue: Y from the partials, per-Rx capacity / dropout / max / mask and
+// the gradient parts; the last CTA reduces the block sums into the loss.
+template <int CB>
+__global__ void __launch_bounds__(256) k_epilogue(ObjArgs a, int kspl, const float *Ypart,
+                                                  float *G1, float *G2, double *partials,
+                                                  unsigned *counter, float *scal) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
   double sum_max = 0.0, sum_sq = 0.0;
-  if (live) {
+  if (r < a.R) {
+    c2 y[CB];
     float cap[CB], amp[CB];
     int arg = 0;
     float mx = -1.f;
 #pragma unroll
     for (int c = 0; c < CB; c++) {
-      if (c >= C) { cap[c] = 0.f; amp[c] = 0.f; continue; }
+      y[c] = {0.f, 0.f};
+      if (c >= a.C) { cap[c] = 0.f; amp[c] = 0.f; continue; }
+      for (int sp = 0; sp < kspl; sp++) {
+        c2 v = ld2(Ypart, ((size_t)sp * a.C + c) * a.R + r);
+        y[c].x += v.x;
+        y[c].y += v.y;
+      }
       amp[c] = sqrtf(y[c].x * y[c].x + y[c].y * y[c].y);
-      float a = amp[c] + kEps;
-      float v = log2f(1.0f + a * a / kN0);
-      if (drop && drop[c]) v = 0.f;
+      const float aa = amp[c] + kEps;
+      float v = log2f(1.0f + aa * aa / kN0);
+      if (a.drop && a.drop[c]) v = 0.f;
       cap[c] = v;
       if (v > mx) { mx = v; arg = c; }  // first index of the maximum
-      if (recv_amp) recv_amp[(size_t)c * R + r] = amp[c];
+      if (a.recv_amp) a.recv_amp[(size_t)c * a.R + r] = amp[c];
     }
     sum_max = mx;
 #pragma unroll
     for (int c = 0; c < CB; c++) {
-      if (c >= C) continue;
-      bool dropped = drop && drop[c];
-      float msk = (cap[c] != mx) ? cap[c] : 0.f;  // (cap' * mask)
+      if (c >= a.C) continue;
+      const bool dropped = a.drop && a.drop[c];
+      const float msk = (cap[c] != mx) ? cap[c] : 0.f;  // cap' * mask
       sum_sq += (double)msk * msk;
-      float a = amp[c] + kEps;
-      float dcap = (2.0f * a / kN0) / ((1.0f + a * a / kN0)) * kInvLn2;
-      float g1 = (c == arg) ? -w : 0.f;
-      float g2 = msk;
+      const float aa = amp[c] + kEps;
+      const float dcap = (2.0f * aa / kN0) / (1.0f + aa * aa / kN0) * kInvLn2;
+      float g1 = (c == arg) ? -a.w : 0.f, g2 = msk;
       if (dropped) { g1 = 0.f; g2 = 0.f; }
-      float sc = amp[c] > 0.f ? dcap / amp[c] : 0.f;
-      reinterpret_cast<float2 *>(G1)[(size_t)c * R + r] = make_float2(g1 * sc * y[c].x, g1 * sc * y[c].y);
+      const float sc = amp[c] > 0.f ? dcap / amp[c] : 0.f;
+      reinterpret_cast<float2 *>(G1)[(size_t)c * a.R + r] =
+          make_float2(g1 * sc * y[c].x, g1 * sc * y[c].y);
       if (G2)
-        reinterpret_cast<float2 *>(G2)[(size_t)c * R + r] = make_float2(g2 * sc * y[c].x, g2 * sc * y[c].y);
+        reinterpret_cast<float2 *>(G2)[(size_t)c * a.R + r] =
+            make_float2(g2 * sc * y[c].x, g2 * sc * y[c].y);
     }
   }
-  // block partials (deterministic order: warp shuffles then warps in order)
   for (int o = 16; o > 0; o >>= 1) {
     sum_max += __shfl_xor_sync(0xffffffffu, sum_max, o);
     sum_sq += __shfl_xor_sync(0xffffffffu, sum_sq, o);
   }
-  __shared__ double sp[2][4];
-  int wid = threadIdx.x >> 5;
+  __shared__ double sp[2][8];
+  __shared__ bool last;
+  const int wid = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) { sp[0][wid] = sum_max; sp[1][wid] = sum_sq; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double a = 0, b = 0;
-    for (int i = 0; i < 4; i++) { a += sp[0][i]; b += sp[1][i]; }
-    partials[2 * blockIdx.x] = a;
-    partials[2 * blockIdx.x + 1] = b;
+    double x = 0, z = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) { x += sp[0][i]; z += sp[1][i]; }
+    partials[2 * blockIdx.x] = x;
+    partials[2 * blockIdx.x + 1] = z;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
-}
-
-__global__ void k_scalars(const double *partials, int nblocks, float w, float *loss,
-                          float *inv_nrm) {
-  __shared__ double s[2][256];
-  double a = 0, b = 0;
-  for (int i = threadIdx.x; i < nblocks; i += blockDim.x) { a += partials[2 * i]; b += partials[2 * i + 1]; }
-  s[0][threadIdx.x] = a;
-  s[1][threadIdx.x] = b;
   __syncthreads();
-  for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-    if (threadIdx.x < h) { s[0][threadIdx.x] += s[0][threadIdx.x + h]; s[1][threadIdx.x] += s[1][threadIdx.x + h]; }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    double nrm = sqrt(s[1][0]);
-    if (loss) *loss = (float)(-(double)w * s[0][0] + nrm);
-    *inv_nrm = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double x = 0, z = 0;
+    const volatile double *pp = partials;
+    for (int b = 0; b < (int)gridDim.x; b++) { x += pp[2 * b]; z += pp[2 * b + 1]; }
+    const double nrm = sqrt(z);
+    if (a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
+    scal[0] = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+    *counter = 0u;  // ready for the next call
   }
 }
 
-// G_U[c, row] = sum_r G[c,r] conj(Hrow[row, r]) over rows of [H_r; H_d]:
-// a warp owns RPW rows, lanes stride over r, G staged in shared memory.
-template <int CB, int RPW>
-__global__ void __launch_bounds__(128) k_pass2(const float *Hr, const float *Hd, int M, int S,
-                                               int R, int C, const float *G1, const float *G2,
-                                               const float *inv_nrm, float *GU) {
-  constexpr int TR = CB >= 64 ? 64 : 128;
+// pass 2: partial G_U[c, k] = sum_r G[c, r] conj(row_k[r]) over an r-range;
+// one warp per row, lanes stride over columns, G staged in shared memory.
+template <int CB>
+__global__ void __launch_bounds__(256) k_pass2(ObjArgs a, int M, int K, int rper, const float *G1,
+                                               const float *G2, const float *scal, float *GUp) {
+  constexpr int TR = CB <= 8 ? 256 : (CB <= 32 ? 64 : 32);
   __shared__ c2 sG[CB][TR];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rows = M + S;
-  const int row0 = (blockIdx.x * 4 + warp) * RPW;
-  const float inv = G2 ? *inv_nrm : 0.f;
-  c2 acc[RPW][CB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int k = blockIdx.x * 8 + warp;
+  const int r0 = blockIdx.y * rper, r1 = min(a.R, r0 + rper);
+  const float inv = G2 ? scal[0] : 0.f;
+  const float *row = k < K ? row_ptr(a.Hr, a.Hd, M, a.R, k) : nullptr;
+  c2 acc[CB];
 #pragma unroll
-  for (int q = 0; q < RPW; q++)
-#pragma unroll
-    for (int c = 0; c < CB; c++) acc[q][c] = {0.f, 0.f};
-  for (int r0 = 0; r0 < R; r0 += TR) {
+  for (int c = 0; c < CB; c++) acc[c] = {0.f, 0.f};
+  for (int rc = r0; rc < r1; rc += TR) {
+    const int rn = min(TR, r1 - rc);
     __syncthreads();
     for (int i = threadIdx.x; i < CB * TR; i += blockDim.x) {
-      int c = i / TR, rr = i % TR;
+      const int c = i / TR, rr = i % TR;
       c2 g = {0.f, 0.f};
-      if (c < C && r0 + rr < R) {
-        g = ld2(G1, (size_t)c * R + r0 + rr);
+      if (c < a.C && rr < rn) {
+        g = ld2(G1, (size_t)c * a.R + rc + rr);
         if (G2) {
-          c2 g2 = ld2(G2, (size_t)c * R + r0 + rr);
-          g.x = fmaf(g2.x, inv, g.x);
-          g.y = fmaf(g2.y, inv, g.y);
+          const c2 h = ld2(G2, (size_t)c * a.R + rc + rr);
+          g.x = fmaf(h.x, inv, g.x);
+          g.y = fmaf(h.y, inv, g.y);
         }
       }
       sG[c][rr] = g;
     }
     __syncthreads();
+    if (row) {
+#pragma unroll 4
+      for (int rr = lane; rr < rn; rr += 32) {
+        const c2 h = ld2(row, (size_t)(rc + rr));
 #pragma unroll
-    for (int q = 0; q < RPW; q++) {
-      int row = row0 + q;
-      if (row >= rows) break;
-      const float *base = row < M ? Hr + (size_t)row * R * 2 : Hd + (size_t)(row - M) * R * 2;
-#pragma unroll
-      for (int j = 0; j < TR / 32; j++) {
-        int rr = lane + 32 * j;
-        if (r0 + rr >= R) break;
-        c2 h = ld2(base, (size_t)(r0 + rr));
-#pragma unroll
-        for (int c = 0; c < CB; c++) macc(acc[q][c], sG[c][rr], h);
+        for (int c = 0; c < CB; c++) macc(acc[c], sG[c][rr], h);
       }
     }
   }
 #pragma unroll
-  for (int q = 0; q < RPW; q++) {
-    int row = row0 + q;
-#pragma unroll
-    for (int c = 0; c < CB; c++) {
-      float x = acc[q][c].x, y = acc[q][c].y;
-      for (int o = 16; o > 0; o >>= 1) {
-        x += __shfl_xor_sync(0xffffffffu, x, o);
-        y += __shfl_xor_sync(0xffffffffu, y, o);
-      }
-      if (lane == 0 && row < rows && c < C)
-        reinterpret_cast<float2 *>(GU)[(size_t)c * rows + row] = make_float2(x, y);
+  for (int c = 0; c < CB; c++) {
+    float x = acc[c].x, y = acc[c].y;
+    for (int o = 16; o > 0; o >>= 1) {
+      x += __shfl_xor_sync(0xffffffffu, x, o);
+      y += __shfl_xor_sync(0xffffffffu, y, o);
     }
+    if (lane == 0 && row && c < a.C)
+      reinterpret_cast<float2 *>(GUp)[((size_t)blockIdx.y * a.C + c) * K + k] = make_float2(x, y);
+  }
+}
+
+__device__ __forceinline__ c2 gu_sum(const float *GUp, int rspl, int C, int K, int c, int k) {
+  c2 g = {0.f, 0.f};
+  for (int sp = 0; sp < rspl; sp++) {
+    const c2 v = ld2(GUp, ((size_t)sp * C + c) * K + k);
+    g.x += v.x;
+    g.y += v.y;
+  }
+  return g;
+}
+
+// final: blocks [0, nb_phi) give dphi[m] = -sum_c Im(conj(G_U) U); the rest
+// give G_W[c, s] = G_U[c, M+s] + sum_m G_U[c, m] e^{-j phi'_m} conj(H_a[s, m])
+// with one warp per (c, s).
+__global__ void __launch_bounds__(256) k_final(ObjArgs a, int M, int K, int rspl, int nb_phi,
+                                               const float *GUp) {
+  if ((int)blockIdx.x < nb_phi) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M || !a.grad_phi) return;
+    float s = 0.f;
+    for (int c = 0; c < a.C; c++) {
+      const c2 g = gu_sum(GUp, rspl, a.C, K, c, m);
+      const c2 u = coef_u(a.W, a.Ha, a.phi, a.max_phase, a.S, M, c, m);
+      s += g.x * u.y - g.y * u.x;  // Im(conj(g) u)
+    }
+    a.grad_phi[m] = -s;
+    return;
+  }
+  if (!a.grad_W) return;
+  const int wid = ((blockIdx.x - nb_phi) * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (wid >= a.C * a.S) return;
+  const int c = wid / a.S, s = wid % a.S;
+  c2 acc = {0.f, 0.f};
+  for (int m = lane; m < M; m += 32) {
+    const c2 g = gu_sum(GUp, rspl, a.C, K, c, m);
+    const float p = py_mod(__ldg(a.phi + m), a.max_phase);
+    float sn, cs;
+    sincosf(p, &sn, &cs);
+    const c2 gv = {g.x * cs + g.y * sn, g.y * cs - g.x * sn};  // g e^{-j p}
+    macc(acc, gv, ld2(a.Ha, (size_t)s * M + m));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+  }
+  if (lane == 0) {
+    const c2 d = gu_sum(GUp, rspl, a.C, K, c, M + s);
+    reinterpret_cast<float2 *>(a.grad_W)[(size_t)c * a.S + s] = make_float2(acc.x + d.x, acc.y + d.y);
   }
 }
 
 // grad_Y = G1 + G2 / ||masked||
-__global__ void k_grad_y(const float *G1, const float *G2, const float *inv_nrm, long long n,
+__global__ void k_grad_y(const float *G1, const float *G2, const float *scal, long long n,
                          float *out) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  float inv = G2 ? *inv_nrm : 0.f;
+  const float inv = G2 ? scal[0] : 0.f;
   c2 g = ld2(G1, i);
   if (G2) {
-    c2 h = ld2(G2, i);
+    const c2 h = ld2(G2, i);
     g.x = fmaf(h.x, inv, g.x);
     g.y = fmaf(h.y, inv, g.y);
   }
   reinterpret_cast<float2 *>(out)[i] = make_float2(g.x, g.y);
-}
-
-// dphi[m] = -sum_c Im(conj(G_U[c,m]) U[c,m])
-__global__ void k_dphi(const float *GU, const float *U, int M, int S, int C, float *dphi) {
-  int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= M) return;
-  float s = 0.f;
-  for (int c = 0; c < C; c++) {
-    c2 g = ld2(GU, (size_t)c * (M + S) + m), u = ld2(U, (size_t)c * M + m);
-    s += g.x * u.y - g.y * u.x;  // Im(conj(g) u)
-  }
-  dphi[m] = -s;
-}
-
-// G_W[c,s] = G_U[c, M+s] + sum_m G_U[c,m] exp(-j phi'_m) conj(H_a[s,m]); one warp per (c,s)
-__global__ void k_gradw(const float *GU, const float *Ha, const float *phi, float max_phase,
-                        int S, int M, int C, float *GW) {
-  int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (wid >= C * S) return;
-  int c = wid / S, s = wid % S;
-  c2 acc = {0.f, 0.f};
-  if (Ha) {
-    for (int m = lane; m < M; m += 32) {
-      c2 g = ld2(GU, (size_t)c * (M + S) + m);
-      float p = py_mod(phi[m], max_phase);
-      float sn, cs;
-      sincosf(p, &sn, &cs);
-      c2 gv = {g.x * cs + g.y * sn, g.y * cs - g.x * sn};  // g * exp(-j p)
-      macc(acc, gv, ld2(Ha, (size_t)s * M + m));
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-    }
-  }
-  if (lane == 0) {
-    c2 d = ld2(GU, (size_t)c * (M + S) + M + s);
-    reinterpret_cast<float2 *>(GW)[(size_t)c * S + s] = make_float2(acc.x + d.x, acc.y + d.y);
-  }
 }
 
 int cbucket(int C) {
@@ -326,20 +348,45 @@ int cbucket(int C) {
   return b;
 }
 
-template <int CB>
-cudaError_t launch_pass1(int blocks, cudaStream_t st, const float *Hd, const float *W,
-                         const float *Hr, const float *U, int S, int M, int R, int C, float w,
-                         const uint8_t *drop, float *G1, float *G2, double *part, float *amp) {
-  k_pass1<CB><<<blocks, 128, 0, st>>>(Hd, W, Hr, U, S, M, R, C, w, drop, G1, G2, part, amp);
-  return cudaGetLastError();
+constexpr int kTargetBlocks = 152 * 8;
+
+struct Split {
+  int K, kspl, kper, rspl, rper, nb_epi;
+};
+
+Split make_split(int S, int M, int R) {
+  Split sp;
+  sp.K = M + S;
+  const int bx = (R + 31) / 32;
+  sp.kspl = std::max(1, std::min((kTargetBlocks + bx - 1) / bx, (sp.K + 63) / 64));
+  sp.kper = (sp.K + sp.kspl - 1) / sp.kspl;
+  sp.kspl = (sp.K + sp.kper - 1) / sp.kper;
+  const int by = (sp.K + 7) / 8;
+  sp.rspl = std::max(1, std::min((kTargetBlocks + by - 1) / by, (R + 255) / 256));
+  sp.rper = (R + sp.rspl - 1) / sp.rspl;
+  sp.rspl = (R + sp.rper - 1) / sp.rper;
+  sp.nb_epi = (R + 255) / 256;
+  return sp;
 }
 
-template <int CB, int RPW>
-cudaError_t launch_pass2(cudaStream_t st, const float *Hr, const float *Hd, int M, int S, int R,
-                         int C, const float *G1, const float *G2, const float *inv, float *GU) {
-  int rows = M + S;
-  int blocks = (rows + 4 * RPW - 1) / (4 * RPW);
-  k_pass2<CB, RPW><<<blocks, 128, 0, st>>>(Hr, Hd, M, S, R, C, G1, G2, inv, GU);
+template <int CB>
+cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *Ypart, float *G1, float *G2,
+                   double *part, unsigned *counter, float *scal, float *GUp, cudaStream_t st) {
+  dim3 g1((a.R + 31) / 32, sp.kspl);
+  k_pass1<CB><<<g1, 256, 0, st>>>(a, M, sp.K, sp.kper, Ypart);
+  k_epilogue<CB><<<sp.nb_epi, 256, 0, st>>>(a, sp.kspl, Ypart, G1, G2, part, counter, scal);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (a.grad_Y) {
+    const long long n = (long long)a.C * a.R;
+    k_grad_y<<<(int)((n + 255) / 256), 256, 0, st>>>(G1, G2, scal, n, a.grad_Y);
+  }
+  if (!a.grad_W && !a.grad_phi) return cudaGetLastError();
+  dim3 g2((sp.K + 7) / 8, sp.rspl);
+  k_pass2<CB><<<g2, 256, 0, st>>>(a, M, sp.K, sp.rper, G1, G2, scal, GUp);
+  const int nb_phi = (a.grad_phi && M > 0) ? (M + 255) / 256 : 0;
+  const int nb_gw = a.grad_W ? (a.C * a.S * 32 + 255) / 256 : 0;
+  if (nb_phi + nb_gw > 0) k_final<<<nb_phi + nb_gw, 256, 0, st>>>(a, M, sp.K, sp.rspl, nb_phi, GUp);
   return cudaGetLastError();
 }
 
@@ -347,74 +394,39 @@ cudaError_t launch_pass2(cudaStream_t st, const float *Hr, const float *Hd, int 
 
 ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  const Split sp = make_split(S, M, R);
   ObjScratchLayout L;
-  int nb = (R + 127) / 128;
   size_t o = 0;
-  L.U = o; o += al(8 * (size_t)C * std::max(M, 1));
+  L.inv = o; o += 256;                                    // control block (see header)
+  L.U = o; o += al(8 * (size_t)sp.kspl * C * R);          // Y partials
   L.G1 = o; o += al(8 * (size_t)C * R);
   L.G2 = o; o += al(8 * (size_t)C * R);
-  L.part = o; o += al(16 * (size_t)nb);
-  L.GU = o; o += al(8 * (size_t)C * (std::max(M, 0) + S));
-  L.inv = o; o += al(16);
+  L.part = o; o += al(16 * (size_t)sp.nb_epi);
+  L.GU = o; o += al(8 * (size_t)sp.rspl * C * sp.K);      // G_U partials
   L.total = o;
   return L;
 }
 
-cudaError_t obj_run(const ObjArgs &a, char *scratch, cudaStream_t st) {
-  const ObjScratchLayout L = obj_scratch_layout(a.S, a.M, a.R, a.C);
+cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
+  ObjArgs a = a0;
   const bool ms = a.Ha && a.Hr;
   const int M = ms ? a.M : 0;
-  float *U = reinterpret_cast<float *>(scratch + L.U);
+  if (!ms) { a.Ha = nullptr; a.Hr = nullptr; a.grad_phi = nullptr; }
+  const ObjScratchLayout L = obj_scratch_layout(a.S, M, a.R, a.C);
+  const Split sp = make_split(a.S, M, a.R);
+  float *Ypart = reinterpret_cast<float *>(scratch + L.U);
   float *G1 = reinterpret_cast<float *>(scratch + L.G1);
   float *G2 = a.C > 1 ? reinterpret_cast<float *>(scratch + L.G2) : nullptr;
   double *part = reinterpret_cast<double *>(scratch + L.part);
-  float *GU = reinterpret_cast<float *>(scratch + L.GU);
-  float *inv = reinterpret_cast<float *>(scratch + L.inv);
-  cudaError_t e;
-  if (ms) {
-    dim3 g((M + 255) / 256, a.C);
-    k_prep<<<g, 256, 0, st>>>(a.W, a.Ha, a.phi, a.max_phase, a.S, M, a.C, U);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-  const int nb = (a.R + 127) / 128;
-  const float *Hr = ms ? a.Hr : nullptr;
+  float *GUp = reinterpret_cast<float *>(scratch + L.GU);
+  float *scal = reinterpret_cast<float *>(scratch + L.inv);
+  unsigned *counter = reinterpret_cast<unsigned *>(scratch + L.inv + 32);
   switch (cbucket(a.C)) {
-#define P1(CB) case CB: e = launch_pass1<CB>(nb, st, a.Hd, a.W, Hr, U, a.S, M, a.R, a.C, a.w, a.drop, G1, G2, part, a.recv_amp); break;
-    P1(1) P1(2) P1(4) P1(8) P1(16) P1(32) P1(64)
-#undef P1
+#define CASE(CB) case CB: return run_cb<CB>(a, sp, M, Ypart, G1, G2, part, counter, scal, GUp, st);
+    CASE(1) CASE(2) CASE(4) CASE(8) CASE(16) CASE(32) CASE(64)
+#undef CASE
     default: return cudaErrorInvalidValue;
   }
-  if (e != cudaSuccess) return e;
-  k_scalars<<<1, 256, 0, st>>>(part, nb, a.w, a.loss, inv);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (a.grad_Y) {
-    long long n = (long long)a.C * a.R;
-    k_grad_y<<<(int)((n + 255) / 256), 256, 0, st>>>(G1, G2, inv, n, a.grad_Y);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-  if (!a.grad_W && !a.grad_phi) return cudaSuccess;
-  switch (cbucket(a.C)) {
-    case 1: e = launch_pass2<1, 8>(st, Hr, a.Hd, M, a.S, a.R, a.C, G1, G2, inv, GU); break;
-    case 2: e = launch_pass2<2, 4>(st, Hr, a.Hd, M, a.S, a.R, a.C, G1, G2, inv, GU); break;
-    case 4: e = launch_pass2<4, 2>(st, Hr, a.Hd, M, a.S, a.R, a.C, G1, G2, inv, GU); break;
-    case 8: e = launch_pass2<8, 1>(st, Hr, a.Hd, M, a.S, a.R, a.C, G1, G2, inv, GU); break;
-    case 16: e = launch_pass2<16, 1>(st, Hr, a.Hd, M, a.S, a.R, a.C, G1, G2, inv, GU); break;
-    case 32: e = launch_pass2<32, 1>(st, Hr, a.Hd, M, a.S, a.R, a.C, G1, G2, inv, GU); break;
-    case 64: e = launch_pass2<64, 1>(st, Hr, a.Hd, M, a.S, a.R, a.C, G1, G2, inv, GU); break;
-    default: return cudaErrorInvalidValue;
-  }
-  if (e != cudaSuccess) return e;
-  if (a.grad_phi && ms) {
-    k_dphi<<<(M + 255) / 256, 256, 0, st>>>(GU, U, M, a.S, a.C, a.grad_phi);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-  if (a.grad_W) {
-    int warps = a.C * a.S;
-    k_gradw<<<(warps * 32 + 255) / 256, 256, 0, st>>>(GU, ms ? a.Ha : nullptr, a.phi, a.max_phase,
-                                                      a.S, M, a.C, a.grad_W);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  }
-  return cudaSuccess;
 }
 
 namespace {

@@ -13,10 +13,14 @@ struct ObjArgs {
   float *loss, *grad_W, *grad_phi, *recv_amp, *grad_Y;
 };
 
-// byte offsets of the scratch regions for one problem size
+// Byte offsets of the scratch regions for one problem size.  The first 256
+// bytes are a control block at a fixed offset: a float (1/||masked||) at 0 and
+// the last-CTA arrival counter (uint32) at 32.  The counter must be zero
+// before the first call; every call leaves it at zero again.
 struct ObjScratchLayout {
   size_t U, G1, G2, part, GU, inv, total;
 };
+constexpr size_t kObjControlBytes = 256;
 
 ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C);
 // enqueue one evaluation on `st`; scratch must hold layout.total bytes
