@@ -143,57 +143,70 @@ def run_reference(args, rank, world):
 
 
 def objective_bench(torch, steps, flush):
-    """Plain objective fwd+bwd, S=16 M=1024 R=4096 C=1, through the C ABI."""
+    """Plain objective fwd+bwd, S=16 M=1024 R=4096 C=1, through the C ABI.
+
+    Eight independent channel sets (274 MB, more than L2) are evaluated in
+    turn, so every evaluation streams its H_r from HBM; the eight calls are
+    captured once in a CUDA graph and replayed, which removes the host-side
+    launch cost from the device timing."""
     import ctypes as C
 
     from automs_gb300._lib import call
     rng = np.random.Generator(np.random.PCG64(1))
     S, M, R = 16, 1024, 4096
+    NSET = 8
     lam = 3e8 / 60e9
 
     def cn(*sh):
         d = rng.uniform(2.0, 15.0, size=sh)
         g = (rng.normal(size=sh) + 1j * rng.normal(size=sh)) / np.sqrt(2)
         return torch.as_tensor((g * lam / (4 * np.pi * d)).astype(np.complex64), device="cuda")
-    Hd, Ha, Hr = cn(S, R), cn(S, M), cn(M, R)
+    sets = [(cn(S, R), cn(S, M), cn(M, R)) for _ in range(NSET)]
     phi = torch.as_tensor(rng.uniform(0, 2 * np.pi, M).astype(np.float32), device="cuda")
     wv = rng.normal(size=S) + 1j * rng.normal(size=S)
     W = torch.as_tensor((wv / np.linalg.norm(wv)).astype(np.complex64)[None], device="cuda")
-    loss = torch.empty((), device="cuda")
-    gW = torch.empty_like(W)
-    gphi = torch.empty_like(phi)
+    loss = torch.empty(NSET, device="cuda")
+    gW = torch.empty(NSET, 1, S, dtype=torch.complex64, device="cuda")
+    gphi = torch.empty(NSET, M, device="cuda")
     P = lambda t: C.c_void_p(t.data_ptr())
-    st = torch.cuda.current_stream()
+    st = torch.cuda.Stream()
 
-    def once():
-        call("ams_objective_fwd_bwd", P(Hd), P(Ha), P(Hr), P(phi), float(2 * np.pi), P(W), S, M, R,
-             1, 1.0 / R, C.c_void_p(0), P(loss), P(gW), P(gphi), C.c_void_p(0), C.c_void_p(0),
-             C.c_void_p(st.cuda_stream))
-    for _ in range(5):
-        once()
-    torch.cuda.synchronize()
-    times = []
-    for _ in range(steps):
-        flush()
+    def evals():
+        for i, (Hd, Ha, Hr) in enumerate(sets):
+            call("ams_objective_fwd_bwd", P(Hd), P(Ha), P(Hr), P(phi), float(2 * np.pi), P(W), S,
+                 M, R, 1, 1.0 / R, C.c_void_p(0), P(loss[i]), P(gW[i]), P(gphi[i]),
+                 C.c_void_p(0), C.c_void_p(0), C.c_void_p(st.cuda_stream))
+    with torch.cuda.stream(st):
+        for _ in range(3):
+            evals()
+        st.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=st):
+            evals()
+        for _ in range(3):
+            g.replay()
+        st.synchronize()
+        reps = max(1, steps // NSET)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        flush()
         e0.record(st)
-        once()
+        for _ in range(reps):
+            g.replay()
         e1.record(st)
-        times.append((e0, e1))
-    torch.cuda.synchronize()
-    ms = [a.elapsed_time(b) for a, b in times]
-    t = sum(ms) / len(ms)
+        st.synchronize()
+    t = e0.elapsed_time(e1) / (reps * NSET)
     bytes_alg = 8 * (R * M + M * S + R * S)
     hbm, kind = peaks()
     achieved = bytes_alg / (t * 1e-3) / 1e9
-    # host side: the same evaluation from host buffers (H2D of phi and w, D2H of loss + grads)
     return {"metric": "objective+grad evals/s", "value": 1e3 / t, "unit": "evals/s",
-            "ms_per_eval": t, "config": {"S": S, "M": M, "R": R, "C": 1, "l2": "flushed"},
+            "ms_per_eval": t, "evals": reps * NSET,
+            "config": {"S": S, "M": M, "R": R, "C": 1,
+                       "l2": "8 channel sets (274 MB) evaluated in turn, CUDA-graph replay"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None,
                          "algorithmic_bytes": bytes_alg, "peak_kind": kind},
-            "gpu_launches_per_eval": 6}
+            "gpu_launches_per_eval": 4}
 
 
 def main():
