@@ -67,6 +67,8 @@ SIGNATURES = {
     "ams_trace_export_paths": (_I, [_P, _P, _I, C.POINTER(_I), _E, _S]),
     "ams_objective_fwd_bwd": (_I, [_P, _P, _P, _P, _F, _P, _I, _I, _I, _I, _F, _P, _P, _P, _P,
                                    _P, _P, _P, _E, _S]),
+    "ams_objective_fwd_bwd_noalloc": (_I, [_P, _P, _P, _P, _F, _P, _I, _I, _I, _I, _F, _P, _P,
+                                           _P, _P, _P, _P, _P, _E, _S]),
     "ams_objective_recv": (_I, [_P, _P, _P, _P, _F, _P, _I, _I, _I, _I, _P, _P, _E, _S]),
     "ams_coverage_db": (_I, [_P, _I, _I, _F, _F, _P, _P, _E, _S]),
     "ams_scratch_bytes": (C.c_ulonglong, []),

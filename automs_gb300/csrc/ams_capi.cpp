@@ -545,6 +545,36 @@ ams_status ams_objective_fwd_bwd(const float *H_d, const float *H_a, const float
   return AMS_OK;
 }
 
+ams_status ams_objective_fwd_bwd_noalloc(const float *H_d, const float *H_a, const float *H_r,
+                                         const float *phi, float max_phase, const float *W, int S,
+                                         int M, int R, int C, float w, const uint8_t *drop,
+                                         float *loss, float *grad_W, float *grad_phi,
+                                         float *grad_Y, float *recv_amp, void *stream,
+                                         char *errbuf, size_t errlen) {
+  ams_status v = obj_validate(H_d, H_a, H_r, phi, max_phase, W, S, M, R, C, errbuf, errlen);
+  if (v != AMS_OK) return v;
+  if (!loss) { set_err(errbuf, errlen, "loss output is NULL"); return AMS_ERR_ARG; }
+  if (grad_phi && !H_a) { set_err(errbuf, errlen, "grad_phi needs a metasurface hop"); return AMS_ERR_ARG; }
+  const bool ms = H_a != nullptr;
+  const ObjScratchLayout L = obj_scratch_layout(S, ms ? M : 0, R, C);
+  if (L.total > (size_t)AMS_OBJECTIVE_NOALLOC_MAX_SCRATCH) {
+    set_err(errbuf, errlen,
+            "problem needs %zu bytes of scratch, above the fixed %u bytes of the "
+            "allocation-free entry point (S=%d M=%d R=%d C=%d)",
+            L.total, (unsigned)AMS_OBJECTIVE_NOALLOC_MAX_SCRATCH, S, M, R, C);
+    return AMS_ERR_CAPACITY;
+  }
+  char *scr = nullptr;
+  CK(obj_noalloc_scratch(&scr));
+  cudaStream_t st = (cudaStream_t)stream;
+  // the control block (arrival counter) must be zero when a call starts
+  CK(cudaMemsetAsync(scr, 0, kObjControlBytes, st));
+  ObjArgs a{H_d, H_a, H_r, phi, W, max_phase, S, ms ? M : 0, R, C, w, drop,
+            loss, grad_W, ms ? grad_phi : nullptr, recv_amp, grad_Y};
+  CK(obj_run(a, scr, st));
+  return AMS_OK;
+}
+
 ams_status ams_objective_recv(const float *H_d, const float *H_a, const float *H_r,
                               const float *phi, float max_phase, const float *W, int S, int M,
                               int R, int C, float *recv_amp, void *stream, char *errbuf,

@@ -24,6 +24,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <mutex>
+#include <vector>
 
 #include "../../include/ams.h"
 #include "objective.h"
@@ -454,4 +455,30 @@ cudaError_t coverage_db_run(const float *H, int S, int R, float threshold, float
                             float *out, cudaStream_t st) {
   k_coverage_db<<<(R + 255) / 256, 256, 0, st>>>(H, S, R, threshold, offset, out);
   return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------
+// Fixed scratch for callers that cannot allocate device memory.  The array
+// is part of the module image: every device that loads the library holds
+// AMS_OBJECTIVE_NOALLOC_MAX_SCRATCH bytes of it until the process exits.
+// Host code must not use the symbol itself as a device address; the address
+// is looked up per device with cudaGetSymbolAddress.
+static __device__ __align__(256) char g_noalloc_scratch[AMS_OBJECTIVE_NOALLOC_MAX_SCRATCH];
+
+cudaError_t obj_noalloc_scratch(char **out) {
+  static std::mutex mu;
+  static std::vector<char *> per_device;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)per_device.size() <= dev) per_device.resize(dev + 1, nullptr);
+  if (!per_device[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // with `dev` current
+    if (e != cudaSuccess) return e;
+    per_device[dev] = static_cast<char *>(p);
+  }
+  *out = per_device[dev];
+  return cudaSuccess;
 }

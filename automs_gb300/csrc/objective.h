@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/ams.h"
+
 struct ObjArgs {
   const float *Hd, *Ha, *Hr, *phi, *W;
   float max_phase;
@@ -27,3 +29,6 @@ ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C);
 cudaError_t obj_run(const ObjArgs &a, char *scratch, cudaStream_t st);
 cudaError_t coverage_db_run(const float *H, int S, int R, float threshold, float offset,
                             float *out, cudaStream_t st);
+// scratch of the allocation-free entry point (objective.cu); the first call
+// on a device looks up the array's device address
+cudaError_t obj_noalloc_scratch(char **out);

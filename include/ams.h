@@ -144,6 +144,28 @@ ams_status ams_objective_fwd_bwd(const float *H_d, const float *H_a,
                                  float *grad_Y, float *recv_amp, void *stream,
                                  char *errbuf, size_t errlen);
 
+/* Allocation-free variant of ams_objective_fwd_bwd.  No counterpart in the
+ * reference: it exists for callers that must not allocate device memory,
+ * e.g. code that owns the whole device memory through its own pool, code
+ * inside a CUDA stream capture where cudaMalloc is not allowed, or
+ * latency-critical loops that cannot afford cudaMalloc's implicit
+ * synchronisation.  Same arguments and results as ams_objective_fwd_bwd;
+ * its scratch is a fixed array of AMS_OBJECTIVE_NOALLOC_MAX_SCRATCH bytes
+ * inside the library image (held on every device that loads the library
+ * until the process exits), so the call itself never allocates.  Problems
+ * whose scratch would exceed that size are rejected with AMS_ERR_CAPACITY.
+ * The first call on a device looks the array up for that device; make that
+ * first call before any stream capture.  All calls on a device share the
+ * array, so calls that overlap on the GPU (different streams, threads) race
+ * and give wrong results: serialise them.  The call is asynchronous on
+ * `stream`. */
+#define AMS_OBJECTIVE_NOALLOC_MAX_SCRATCH (16u << 20)
+ams_status ams_objective_fwd_bwd_noalloc(
+    const float *H_d, const float *H_a, const float *H_r, const float *phi,
+    float max_phase, const float *W, int S, int M, int R, int C, float w,
+    const uint8_t *drop, float *loss, float *grad_W, float *grad_phi,
+    float *grad_Y, float *recv_amp, void *stream, char *errbuf, size_t errlen);
+
 /* Received amplitude |Y| [C,R] of the same model (forward only). */
 ams_status ams_objective_recv(const float *H_d, const float *H_a,
                               const float *H_r, const float *phi,
