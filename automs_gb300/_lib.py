@@ -72,6 +72,13 @@ SIGNATURES = {
     "ams_objective_recv": (_I, [_P, _P, _P, _P, _F, _P, _I, _I, _I, _I, _P, _P, _E, _S]),
     "ams_coverage_db": (_I, [_P, _I, _I, _F, _F, _P, _P, _E, _S]),
     "ams_scratch_bytes": (C.c_ulonglong, []),
+    "ams_gemm_bf16": (_I, [_P, _P, _I, _I, _I, _P, _I, _P, _P, _P, _E, _S]),
+    "ams_mlp_create": (_I, [_P, _I, _I, C.c_ulonglong, _P, C.POINTER(_P), _E, _S]),
+    "ams_mlp_destroy": (None, [_P]),
+    "ams_mlp_forward": (_I, [_P, _P, _I, _P, _P, _E, _S]),
+    "ams_mlp_train_step": (_I, [_P, _P, _P, _I, _F, _P, _P, _E, _S]),
+    "ams_mlp_gradients": (_I, [_P, _P, _P, _I, _P, _P, _P, _E, _S]),
+    "ams_mlp_params": (_I, [_P, _P, _I, C.POINTER(C.c_longlong), _P, _E, _S]),
 }
 
 

@@ -607,3 +607,227 @@ unsigned long long ams_scratch_bytes(void) {
 }
 
 }  // extern "C"
+
+// -------------------------------------------------------- surrogate MLP
+#include "gemm_tc.h"
+#include "mlp.h"
+
+struct ams_mlp {
+  MlpDev dev;
+  char *arena = nullptr;
+  ~ams_mlp() {
+    if (arena) cudaFree(arena);
+  }
+};
+
+namespace {
+ams_status mlp_check_err(ams_mlp *m, cudaStream_t st, char *errbuf, size_t errlen) {
+  unsigned e = 0;
+  cudaError_t ce = cudaMemcpyAsync(&e, m->dev.err, 4, cudaMemcpyDeviceToHost, st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+  if (ce != cudaSuccess) {
+    set_err(errbuf, errlen, "MLP: %s", cudaGetErrorString(ce));
+    return AMS_ERR_CUDA;
+  }
+  if (e) {
+    set_err(errbuf, errlen, "tensor-core GEMM timed out waiting (flags 0x%x)", e);
+    cudaMemsetAsync(m->dev.err, 0, 4, st);
+    return AMS_ERR_INTERNAL;
+  }
+  return AMS_OK;
+}
+}  // namespace
+
+extern "C" {
+
+ams_status ams_gemm_bf16(const void *A, const void *B, int M, int N, int K, const float *bias,
+                         int relu, float *C32, void *C16, void *stream, char *errbuf,
+                         size_t errlen) {
+  if (!A || !B || (!C32 && !C16)) { set_err(errbuf, errlen, "null operand"); return AMS_ERR_ARG; }
+  if (M <= 0 || N <= 0 || K <= 0 || M % 128 || N % 64 || K % 64) {
+    set_err(errbuf, errlen, "need M %% 128 == 0, N %% 64 == 0, K %% 64 == 0 (M=%d N=%d K=%d)", M,
+            N, K);
+    return AMS_ERR_ARG;
+  }
+  if (((uintptr_t)A | (uintptr_t)B) & 15) {
+    set_err(errbuf, errlen, "A and B must be 16-byte aligned");
+    return AMS_ERR_ARG;
+  }
+  unsigned *err = nullptr;
+  CK(cudaMallocAsync((void **)&err, 4, (cudaStream_t)stream));
+  CK(cudaMemsetAsync(err, 0, 4, (cudaStream_t)stream));
+  GemmEpilogue ep;
+  ep.bias = bias;
+  ep.relu = relu != 0;
+  ep.out32 = C32;
+  ep.out16 = reinterpret_cast<__nv_bfloat16 *>(C16);
+  ep.ldc = N;
+  cudaError_t e = gemm_bf16_tc(reinterpret_cast<const __nv_bfloat16 *>(A),
+                               reinterpret_cast<const __nv_bfloat16 *>(B), M, N, K, ep, err,
+                               (cudaStream_t)stream);
+  unsigned flags = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, err, 4, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  cudaFreeAsync(err, (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    set_err(errbuf, errlen, "GEMM: %s", cudaGetErrorString(e));
+    return AMS_ERR_CUDA;
+  }
+  if (flags) {
+    set_err(errbuf, errlen, "tensor-core GEMM timed out waiting (flags 0x%x)", flags);
+    return AMS_ERR_INTERNAL;
+  }
+  return AMS_OK;
+}
+
+ams_status ams_mlp_create(const int *dims, int n_dims, int max_batch, unsigned long long seed,
+                          void *stream, ams_mlp **out, char *errbuf, size_t errlen) {
+  if (!out || !dims || n_dims < 2 || n_dims > kMlpMaxLayers + 1 || max_batch <= 0) {
+    set_err(errbuf, errlen, "bad MLP shape");
+    return AMS_ERR_ARG;
+  }
+  *out = nullptr;
+  for (int i = 0; i < n_dims; i++)
+    if (dims[i] <= 0 || (i > 0 && dims[i] % 128)) {
+      set_err(errbuf, errlen, "width %d = %d: widths after the input must be multiples of 128", i,
+              dims[i]);
+      return AMS_ERR_ARG;
+    }
+  ams_mlp *m = new ams_mlp();
+  MlpDev &d = m->dev;
+  d.L = n_dims - 1;
+  for (int i = 0; i < n_dims; i++) {
+    d.d[i] = dims[i];
+    d.dp[i] = i == 0 ? (dims[0] + 63) / 64 * 64 : dims[i];
+  }
+  d.max_bp = (max_batch + 127) / 128 * 128;
+  // one arena
+  size_t total = 0;
+  auto add = [&](size_t b) { size_t o = total; total += al(b); return o; };
+  size_t off_W[kMlpMaxLayers + 1], off_b[kMlpMaxLayers + 1], off_mW[kMlpMaxLayers + 1],
+      off_vW[kMlpMaxLayers + 1], off_mb[kMlpMaxLayers + 1], off_vb[kMlpMaxLayers + 1],
+      off_gW[kMlpMaxLayers + 1], off_gb[kMlpMaxLayers + 1], off_Wb[kMlpMaxLayers + 1],
+      off_Wt[kMlpMaxLayers + 1], off_H[kMlpMaxLayers + 1], off_dZ[kMlpMaxLayers + 1];
+  size_t maxw = 0;
+  for (int l = 1; l <= d.L; l++) {
+    size_t n = (size_t)d.d[l] * d.dp[l - 1];
+    off_W[l] = add(4 * n); off_mW[l] = add(4 * n); off_vW[l] = add(4 * n); off_gW[l] = add(4 * n);
+    off_b[l] = add(4 * d.d[l]); off_mb[l] = add(4 * d.d[l]); off_vb[l] = add(4 * d.d[l]);
+    off_gb[l] = add(4 * d.d[l]);
+    off_Wb[l] = add(2 * n); off_Wt[l] = add(2 * n);
+    off_dZ[l] = add(2 * (size_t)d.max_bp * d.dp[l]);
+    maxw = std::max(maxw, (size_t)std::max(d.dp[l], d.dp[l - 1]));
+  }
+  for (int l = 0; l < d.L; l++) off_H[l] = add(2 * (size_t)d.max_bp * d.dp[l]);
+  size_t off_tA = add(2 * (size_t)d.max_bp * maxw), off_tB = add(2 * (size_t)d.max_bp * maxw);
+  size_t off_Y = add(4 * (size_t)d.max_bp * d.dp[d.L]);
+  size_t off_part = add(8 * 152 * 4), off_err = add(4);
+  cudaError_t e = cudaMalloc(&m->arena, total);
+  if (e != cudaSuccess) {
+    set_err(errbuf, errlen, "MLP arena (%zu bytes): %s", total, cudaGetErrorString(e));
+    delete m;
+    return AMS_ERR_OOM;
+  }
+  char *a = m->arena;
+  for (int l = 1; l <= d.L; l++) {
+    d.W[l] = (float *)(a + off_W[l]); d.mW[l] = (float *)(a + off_mW[l]);
+    d.vW[l] = (float *)(a + off_vW[l]); d.gW[l] = (float *)(a + off_gW[l]);
+    d.b[l] = (float *)(a + off_b[l]); d.mb[l] = (float *)(a + off_mb[l]);
+    d.vb[l] = (float *)(a + off_vb[l]); d.gb[l] = (float *)(a + off_gb[l]);
+    d.Wb[l] = (__nv_bfloat16 *)(a + off_Wb[l]); d.Wt[l] = (__nv_bfloat16 *)(a + off_Wt[l]);
+    d.dZ[l] = (__nv_bfloat16 *)(a + off_dZ[l]);
+  }
+  for (int l = 0; l < d.L; l++) d.H[l] = (__nv_bfloat16 *)(a + off_H[l]);
+  d.tA = (__nv_bfloat16 *)(a + off_tA);
+  d.tB = (__nv_bfloat16 *)(a + off_tB);
+  d.Y = (float *)(a + off_Y);
+  d.part = (double *)(a + off_part);
+  d.err = (unsigned *)(a + off_err);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaMemsetAsync(d.err, 0, 4, st);
+  if ((e = mlp_init(d, (uint32_t)(seed ^ (seed >> 32)), st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+    set_err(errbuf, errlen, "MLP init: %s", cudaGetErrorString(e));
+    delete m;
+    return AMS_ERR_CUDA;
+  }
+  *out = m;
+  return AMS_OK;
+}
+
+void ams_mlp_destroy(ams_mlp *mlp) { delete mlp; }
+
+ams_status ams_mlp_forward(ams_mlp *m, const float *X, int B, float *Y, void *stream, char *errbuf,
+                           size_t errlen) {
+  if (!m || !X || !Y || B <= 0 || B > m->dev.max_bp) {
+    set_err(errbuf, errlen, "bad MLP forward arguments (B=%d)", B);
+    return AMS_ERR_ARG;
+  }
+  CK(mlp_forward(m->dev, X, B, Y, (cudaStream_t)stream));
+  return mlp_check_err(m, (cudaStream_t)stream, errbuf, errlen);
+}
+
+ams_status ams_mlp_train_step(ams_mlp *m, const float *X, const float *T, int B, float lr,
+                              float *loss, void *stream, char *errbuf, size_t errlen) {
+  if (!m || !X || !T || B <= 0 || B > m->dev.max_bp || !(lr >= 0.f)) {
+    set_err(errbuf, errlen, "bad MLP training arguments (B=%d)", B);
+    return AMS_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(mlp_forward(m->dev, X, B, nullptr, st));
+  CK(mlp_backward(m->dev, T, B, loss, st));
+  CK(mlp_adam(m->dev, lr, st));
+  return mlp_check_err(m, st, errbuf, errlen);
+}
+
+static void mlp_param_copy(MlpDev &d, float *flat, bool to_flat, bool grads, cudaStream_t st) {
+  size_t o = 0;
+  for (int l = 1; l <= d.L; l++) {
+    float *W = grads ? d.gW[l] : d.W[l];
+    float *b = grads ? d.gb[l] : d.b[l];
+    const size_t dp = sizeof(float) * d.dp[l - 1], dl = sizeof(float) * d.d[l - 1];
+    if (to_flat)
+      cudaMemcpy2DAsync(flat + o, dl, W, dp, dl, d.d[l], cudaMemcpyDeviceToDevice, st);
+    else
+      cudaMemcpy2DAsync(W, dp, flat + o, dl, dl, d.d[l], cudaMemcpyDeviceToDevice, st);
+    o += (size_t)d.d[l] * d.d[l - 1];
+    if (to_flat)
+      cudaMemcpyAsync(flat + o, b, sizeof(float) * d.d[l], cudaMemcpyDeviceToDevice, st);
+    else
+      cudaMemcpyAsync(b, flat + o, sizeof(float) * d.d[l], cudaMemcpyDeviceToDevice, st);
+    o += d.d[l];
+  }
+}
+
+ams_status ams_mlp_gradients(ams_mlp *m, const float *X, const float *T, int B, float *loss,
+                             float *grads, void *stream, char *errbuf, size_t errlen) {
+  if (!m || !X || !T || !grads || B <= 0 || B > m->dev.max_bp) {
+    set_err(errbuf, errlen, "bad MLP gradient arguments");
+    return AMS_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  CK(mlp_forward(m->dev, X, B, nullptr, st));
+  CK(mlp_backward(m->dev, T, B, loss, st));
+  mlp_param_copy(m->dev, grads, true, true, st);
+  CK(cudaGetLastError());
+  return mlp_check_err(m, st, errbuf, errlen);
+}
+
+ams_status ams_mlp_params(ams_mlp *m, float *params, int direction, long long *count, void *stream,
+                          char *errbuf, size_t errlen) {
+  if (!m || (direction != 0 && direction != 1)) {
+    set_err(errbuf, errlen, "bad arguments");
+    return AMS_ERR_ARG;
+  }
+  long long n = 0;
+  for (int l = 1; l <= m->dev.L; l++) n += (long long)m->dev.d[l] * m->dev.d[l - 1] + m->dev.d[l];
+  if (count) *count = n;
+  if (!params) return AMS_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  mlp_param_copy(m->dev, params, direction == 0, false, st);
+  if (direction == 1) CK(mlp_refresh_bf16(m->dev, st));
+  CK(cudaStreamSynchronize(st));
+  return AMS_OK;
+}
+
+}  // extern "C"

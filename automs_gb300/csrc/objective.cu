@@ -61,18 +61,6 @@ __device__ __forceinline__ float py_mod(float a, float b) {
 // coefficient U[c, k]; row k >= M is H_d[k - M, :] with coefficient
 // W[c, k - M].  Y[c, r] = sum_k coef[c, k] row_k[r].
 
-__device__ __forceinline__ c2 coef_u(const float *W, const float *Ha, const float *phi,
-                                     float max_phase, int S, int M, int c, int m) {
-  c2 v = {0.f, 0.f};
-  for (int s = 0; s < S; s++) mac(v, ld2(W, (size_t)c * S + s), ld2(Ha, (size_t)s * M + m));
-  float p = py_mod(__ldg(phi + m), max_phase);  // go.py:133
-  float sn, cs;
-  sincosf(p, &sn, &cs);
-  c2 u = {0.f, 0.f};
-  mac(u, v, c2{cs, sn});
-  return u;
-}
-
 __device__ __forceinline__ const float *row_ptr(const float *Hr, const float *Hd, int M, int R,
                                                 int k) {
   return k < M ? Hr + (size_t)k * R * 2 : Hd + (size_t)(k - M) * R * 2;
@@ -80,9 +68,37 @@ __device__ __forceinline__ const float *row_ptr(const float *Hr, const float *Hd
 
 constexpr int KCHUNK = 256;
 
+// U[c, m] = (sum_s W[c, s] H_a[s, m]) e^{j phi'_m}: one thread per (m, c),
+// loads of H_a coalesced over m, issued 8 at a time
+__global__ void __launch_bounds__(128) k_prep(ObjArgs a, int M, float *U) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (m >= M) return;
+  c2 v = {0.f, 0.f};
+  int s = 0;
+  for (; s + 8 <= a.S; s += 8) {
+    c2 h[8], w[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      h[j] = ld2(a.Ha, (size_t)(s + j) * M + m);
+      w[j] = ld2(a.W, (size_t)c * a.S + s + j);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; j++) mac(v, w[j], h[j]);
+  }
+  for (; s < a.S; s++) mac(v, ld2(a.W, (size_t)c * a.S + s), ld2(a.Ha, (size_t)s * M + m));
+  const float p = py_mod(__ldg(a.phi + m), a.max_phase);  // go.py:133
+  float sn, cs;
+  sincosf(p, &sn, &cs);
+  c2 u = {0.f, 0.f};
+  mac(u, v, c2{cs, sn});
+  reinterpret_cast<float2 *>(U)[(size_t)c * M + m] = make_float2(u.x, u.y);
+}
+
 // pass 1: partial Y over a k-range; lanes = 32 columns, warps share the rows
 template <int CB>
-__global__ void __launch_bounds__(256) k_pass1(ObjArgs a, int M, int K, int kper, float *Ypart) {
+__global__ void __launch_bounds__(256) k_pass1(ObjArgs a, int M, int K, int kper, const float *U,
+                                               float *Ypart) {
   __shared__ c2 sC[KCHUNK][CB];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int r = blockIdx.x * 32 + lane;
@@ -97,8 +113,7 @@ __global__ void __launch_bounds__(256) k_pass1(ObjArgs a, int M, int K, int kper
     for (int i = threadIdx.x; i < kn * CB; i += blockDim.x) {
       const int kk = i / CB, c = i % CB, k = kc + kk;
       c2 v = {0.f, 0.f};
-      if (c < a.C) v = k < M ? coef_u(a.W, a.Ha, a.phi, a.max_phase, a.S, M, c, k)
-                             : ld2(a.W, (size_t)c * a.S + (k - M));
+      if (c < a.C) v = k < M ? ld2(U, (size_t)c * M + k) : ld2(a.W, (size_t)c * a.S + (k - M));
       sC[kk][c] = v;
     }
     __syncthreads();
@@ -163,7 +178,15 @@ __global__ void __launch_bounds__(256) k_epilogue(ObjArgs a, int kspl, const flo
     for (int c = 0; c < CB; c++) {
       y[c] = {0.f, 0.f};
       if (c >= a.C) { cap[c] = 0.f; amp[c] = 0.f; continue; }
-      for (int sp = 0; sp < kspl; sp++) {
+      int sp = 0;
+      for (; sp + 4 <= kspl; sp += 4) {
+        c2 v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = ld2(Ypart, ((size_t)(sp + j) * a.C + c) * a.R + r);
+#pragma unroll
+        for (int j = 0; j < 4; j++) { y[c].x += v[j].x; y[c].y += v[j].y; }
+      }
+      for (; sp < kspl; sp++) {
         c2 v = ld2(Ypart, ((size_t)sp * a.C + c) * a.R + r);
         y[c].x += v.x;
         y[c].y += v.y;
@@ -258,7 +281,7 @@ __global__ void __launch_bounds__(256) k_pass2(ObjArgs a, int M, int K, int rper
     }
     __syncthreads();
     if (row) {
-#pragma unroll 4
+#pragma unroll 8
       for (int rr = lane; rr < rn; rr += 32) {
         const c2 h = ld2(row, (size_t)(rc + rr));
 #pragma unroll
@@ -280,7 +303,15 @@ __global__ void __launch_bounds__(256) k_pass2(ObjArgs a, int M, int K, int rper
 
 __device__ __forceinline__ c2 gu_sum(const float *GUp, int rspl, int C, int K, int c, int k) {
   c2 g = {0.f, 0.f};
-  for (int sp = 0; sp < rspl; sp++) {
+  int sp = 0;
+  for (; sp + 4 <= rspl; sp += 4) {
+    c2 v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) v[j] = ld2(GUp, ((size_t)(sp + j) * C + c) * K + k);
+#pragma unroll
+    for (int j = 0; j < 4; j++) { g.x += v[j].x; g.y += v[j].y; }
+  }
+  for (; sp < rspl; sp++) {
     const c2 v = ld2(GUp, ((size_t)sp * C + c) * K + k);
     g.x += v.x;
     g.y += v.y;
@@ -288,44 +319,69 @@ __device__ __forceinline__ c2 gu_sum(const float *GUp, int rspl, int C, int K, i
   return g;
 }
 
-// final: blocks [0, nb_phi) give dphi[m] = -sum_c Im(conj(G_U) U); the rest
-// give G_W[c, s] = G_U[c, M+s] + sum_m G_U[c, m] e^{-j phi'_m} conj(H_a[s, m])
-// with one warp per (c, s).
-__global__ void __launch_bounds__(256) k_final(ObjArgs a, int M, int K, int rspl, int nb_phi,
-                                               const float *GUp) {
-  if ((int)blockIdx.x < nb_phi) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M || !a.grad_phi) return;
-    float s = 0.f;
-    for (int c = 0; c < a.C; c++) {
-      const c2 g = gu_sum(GUp, rspl, a.C, K, c, m);
-      const c2 u = coef_u(a.W, a.Ha, a.phi, a.max_phase, a.S, M, c, m);
-      s += g.x * u.y - g.y * u.x;  // Im(conj(g) u)
+// final: each CTA owns 32 metasurface rows.  It reduces their G_U partials,
+// writes dphi[m] = -sum_c Im(conj(G_U) U) and the partial sums
+// sum_m G_U[c,m] e^{-j phi'_m} conj(H_a[s,m]) of dL/dW; the last CTA adds the
+// CTAs' partials and the H_d rows G_U[c, M+s] into grad_W.
+template <int CB>
+__global__ void __launch_bounds__(256) k_final(ObjArgs a, int M, int K, int rspl, const float *U,
+                                               const float *GUp, float *gw_part,
+                                               unsigned *counter) {
+  __shared__ c2 gu[CB][32];
+  __shared__ c2 ph[32];
+  __shared__ bool last;
+  const int m0 = blockIdx.x * 32;
+  const int t = threadIdx.x;
+  const int nm = max(0, min(32, M - m0));
+  for (int i = t; i < CB * 32; i += blockDim.x) {
+    const int c = i / 32, j = i % 32;
+    gu[c][j] = (c < a.C && j < nm) ? gu_sum(GUp, rspl, a.C, K, c, m0 + j) : c2{0.f, 0.f};
+  }
+  if (t < 32) {
+    c2 e = {0.f, 0.f};
+    if (t < nm) {
+      const float p = py_mod(__ldg(a.phi + m0 + t), a.max_phase);
+      sincosf(p, &e.y, &e.x);
     }
-    a.grad_phi[m] = -s;
-    return;
+    ph[t] = e;
+  }
+  __syncthreads();
+  if (a.grad_phi && t < nm) {
+    float sacc = 0.f;
+    for (int c = 0; c < a.C; c++) {
+      const c2 g = gu[c][t], u = ld2(U, (size_t)c * M + m0 + t);
+      sacc += g.x * u.y - g.y * u.x;  // Im(conj(g) u)
+    }
+    a.grad_phi[m0 + t] = -sacc;
   }
   if (!a.grad_W) return;
-  const int wid = ((blockIdx.x - nb_phi) * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (wid >= a.C * a.S) return;
-  const int c = wid / a.S, s = wid % a.S;
-  c2 acc = {0.f, 0.f};
-  for (int m = lane; m < M; m += 32) {
-    const c2 g = gu_sum(GUp, rspl, a.C, K, c, m);
-    const float p = py_mod(__ldg(a.phi + m), a.max_phase);
-    float sn, cs;
-    sincosf(p, &sn, &cs);
-    const c2 gv = {g.x * cs + g.y * sn, g.y * cs - g.x * sn};  // g e^{-j p}
-    macc(acc, gv, ld2(a.Ha, (size_t)s * M + m));
+  for (int i = t; i < a.C * a.S; i += blockDim.x) {
+    const int c = i / a.S, s2 = i % a.S;
+    c2 acc = {0.f, 0.f};
+    for (int j = 0; j < nm; j++) {
+      const c2 g = gu[c][j], e = ph[j];
+      const c2 gv = {g.x * e.x + g.y * e.y, g.y * e.x - g.x * e.y};  // g e^{-j p}
+      macc(acc, gv, ld2(a.Ha, (size_t)s2 * M + m0 + j));
+    }
+    reinterpret_cast<float2 *>(gw_part)[(size_t)blockIdx.x * a.C * a.S + i] = make_float2(acc.x, acc.y);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+  __threadfence();
+  __syncthreads();
+  if (t == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int i = t; i < a.C * a.S; i += blockDim.x) {
+    const int c = i / a.S, s2 = i % a.S;
+    c2 acc = gu_sum(GUp, rspl, a.C, K, c, M + s2);
+    const volatile float2 *pp = reinterpret_cast<const volatile float2 *>(gw_part);
+    for (int b = 0; b < (int)gridDim.x; b++) {
+      acc.x += pp[(size_t)b * a.C * a.S + i].x;
+      acc.y += pp[(size_t)b * a.C * a.S + i].y;
+    }
+    reinterpret_cast<float2 *>(a.grad_W)[i] = make_float2(acc.x, acc.y);
   }
-  if (lane == 0) {
-    const c2 d = gu_sum(GUp, rspl, a.C, K, c, M + s);
-    reinterpret_cast<float2 *>(a.grad_W)[(size_t)c * a.S + s] = make_float2(acc.x + d.x, acc.y + d.y);
-  }
+  if (t == 0) *counter = 0u;  // ready for the next call
 }
 
 // grad_Y = G1 + G2 / ||masked||
@@ -366,16 +422,21 @@ Split make_split(int S, int M, int R) {
   sp.rspl = std::max(1, std::min((kTargetBlocks + by - 1) / by, (R + 255) / 256));
   sp.rper = (R + sp.rspl - 1) / sp.rspl;
   sp.rspl = (R + sp.rper - 1) / sp.rper;
-  sp.nb_epi = (R + 255) / 256;
+  sp.nb_epi = (R + 127) / 128;
   return sp;
 }
 
 template <int CB>
-cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *Ypart, float *G1, float *G2,
-                   double *part, unsigned *counter, float *scal, float *GUp, cudaStream_t st) {
+cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *U, float *Ypart, float *G1,
+                   float *G2, double *part, unsigned *counter, float *scal, float *GUp,
+                   float *gw_part, cudaStream_t st) {
+  if (M > 0) {
+    dim3 gp((M + 127) / 128, a.C);
+    k_prep<<<gp, 128, 0, st>>>(a, M, U);
+  }
   dim3 g1((a.R + 31) / 32, sp.kspl);
-  k_pass1<CB><<<g1, 256, 0, st>>>(a, M, sp.K, sp.kper, Ypart);
-  k_epilogue<CB><<<sp.nb_epi, 256, 0, st>>>(a, sp.kspl, Ypart, G1, G2, part, counter, scal);
+  k_pass1<CB><<<g1, 256, 0, st>>>(a, M, sp.K, sp.kper, U, Ypart);
+  k_epilogue<CB><<<sp.nb_epi, 128, 0, st>>>(a, sp.kspl, Ypart, G1, G2, part, counter, scal);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (a.grad_Y) {
@@ -385,9 +446,8 @@ cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *Ypart, float
   if (!a.grad_W && !a.grad_phi) return cudaGetLastError();
   dim3 g2((sp.K + 7) / 8, sp.rspl);
   k_pass2<CB><<<g2, 256, 0, st>>>(a, M, sp.K, sp.rper, G1, G2, scal, GUp);
-  const int nb_phi = (a.grad_phi && M > 0) ? (M + 255) / 256 : 0;
-  const int nb_gw = a.grad_W ? (a.C * a.S * 32 + 255) / 256 : 0;
-  if (nb_phi + nb_gw > 0) k_final<<<nb_phi + nb_gw, 256, 0, st>>>(a, M, sp.K, sp.rspl, nb_phi, GUp);
+  const int nbf = std::max(1, (M + 31) / 32);
+  k_final<CB><<<nbf, 256, 0, st>>>(a, M, sp.K, sp.rspl, U, GUp, gw_part, counter + 1);
   return cudaGetLastError();
 }
 
@@ -399,6 +459,8 @@ ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
   ObjScratchLayout L;
   size_t o = 0;
   L.inv = o; o += 256;                                    // control block (see header)
+  L.Um = o; o += al(8 * (size_t)C * std::max(M, 1));      // U = (W H_a) e^{j phi'}
+  L.gw = o; o += al(8 * (size_t)std::max(1, (M + 31) / 32) * C * S);  // dL/dW partials
   L.U = o; o += al(8 * (size_t)sp.kspl * C * R);          // Y partials
   L.G1 = o; o += al(8 * (size_t)C * R);
   L.G2 = o; o += al(8 * (size_t)C * R);
@@ -422,8 +484,10 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
   float *GUp = reinterpret_cast<float *>(scratch + L.GU);
   float *scal = reinterpret_cast<float *>(scratch + L.inv);
   unsigned *counter = reinterpret_cast<unsigned *>(scratch + L.inv + 32);
+  float *Um = reinterpret_cast<float *>(scratch + L.Um);
+  float *gw = reinterpret_cast<float *>(scratch + L.gw);
   switch (cbucket(a.C)) {
-#define CASE(CB) case CB: return run_cb<CB>(a, sp, M, Ypart, G1, G2, part, counter, scal, GUp, st);
+#define CASE(CB) case CB: return run_cb<CB>(a, sp, M, Um, Ypart, G1, G2, part, counter, scal, GUp, gw, st);
     CASE(1) CASE(2) CASE(4) CASE(8) CASE(16) CASE(32) CASE(64)
 #undef CASE
     default: return cudaErrorInvalidValue;

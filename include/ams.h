@@ -180,6 +180,48 @@ ams_status ams_coverage_db(const float *H, int S, int R, float threshold,
                            float offset, float *out, void *stream,
                            char *errbuf, size_t errlen);
 
+/* ------------------------------------------------------ surrogate MLP */
+
+/* BF16 GEMM on the tensor cores (tcgen05): C = A . B^T with A [M,K], B [N,K]
+ * bf16 row-major (device), FP32 accumulation; epilogue adds bias [N] (may be
+ * NULL), applies ReLU if relu != 0, and stores C32 [M,N] float and/or C16
+ * [M,N] bf16 (either may be NULL).  M % 128 == 0, N % 64 == 0, K % 64 == 0.
+ * No counterpart in the reference (building block of the surrogate). */
+ams_status ams_gemm_bf16(const void *A, const void *B, int M, int N, int K,
+                         const float *bias, int relu, float *C32, void *C16,
+                         void *stream, char *errbuf, size_t errlen);
+
+/* Surrogate network that maps a placement descriptor to a coverage-gain map
+ * and screens annealing candidates; it replaces the blind trials of the
+ * reference's NNI tuner (physical_exp_nni_main.py:11-29).  dims[0..n_dims-1]
+ * are the layer widths (input, hidden..., output); every width after the
+ * input must be a multiple of 128.  ReLU between layers, MSE loss, Adam.
+ * Weights are FP32 masters with BF16 copies for the tensor-core GEMMs. */
+typedef struct ams_mlp ams_mlp;
+ams_status ams_mlp_create(const int *dims, int n_dims, int max_batch,
+                          unsigned long long seed, void *stream, ams_mlp **out,
+                          char *errbuf, size_t errlen);
+void ams_mlp_destroy(ams_mlp *mlp);
+/* Y [B, d_out] = net(X [B, d_in]); float device arrays, B <= max_batch. */
+ams_status ams_mlp_forward(ams_mlp *mlp, const float *X, int B, float *Y,
+                           void *stream, char *errbuf, size_t errlen);
+/* One Adam step on the batch (X, T [B, d_out]); loss (device float, may be
+ * NULL) receives the mean squared error before the step. */
+ams_status ams_mlp_train_step(ams_mlp *mlp, const float *X, const float *T,
+                              int B, float lr, float *loss, void *stream,
+                              char *errbuf, size_t errlen);
+/* Gradient of the loss without a step, written to grads (device) in the
+ * parameter layout below. */
+ams_status ams_mlp_gradients(ams_mlp *mlp, const float *X, const float *T,
+                             int B, float *loss, float *grads, void *stream,
+                             char *errbuf, size_t errlen);
+/* Parameters as one float array: for each layer W [d_out, d_in] row-major
+ * then b [d_out].  direction 0 copies out (get), 1 copies in (set).
+ * *count receives the number of floats; params may be NULL to query it. */
+ams_status ams_mlp_params(ams_mlp *mlp, float *params, int direction,
+                          long long *count, void *stream, char *errbuf,
+                          size_t errlen);
+
 /* Device bytes held by the library's internal scratch (all objective calls
  * on this device) -- for leak checks. */
 unsigned long long ams_scratch_bytes(void);
