@@ -97,14 +97,14 @@ class MLP:
 
     def get_params(self):
         p = torch.empty(self.n_params, device="cuda")
-        call("ams_mlp_params", self._h, _ptr(p), 0, C.c_void_p(0), _stream())
+        call("ams_mlp_params", self._h, _ptr(p), 0, None, _stream())
         return p
 
     def set_params(self, p):
         p = p.to(device="cuda", dtype=torch.float32).contiguous()
         if p.numel() != self.n_params:
             raise ValueError("parameter count mismatch")
-        call("ams_mlp_params", self._h, _ptr(p), 1, C.c_void_p(0), _stream())
+        call("ams_mlp_params", self._h, _ptr(p), 1, None, _stream())
 
     def fit(self, X, T, epochs=10, batch=1024, lr=1e-3, seed=0, lr_decay=1.0):
         """Minibatch Adam over (X, T); returns the per-epoch mean losses."""
