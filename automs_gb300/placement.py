@@ -1,0 +1,248 @@
+"""Metasurface placement study: ray-traced gain maps, surrogate screening and
+simulated annealing.
+
+Reference behaviour: one NNI trial (physical_exp_nni_model.py:7-149) places a
+metasurface on a wall (gen_sth_from_wall + gen_ms, go.py:388-477), builds the
+AP->Rx, AP->MS and MS->Rx channels (build_channels, go.py:1135-1247),
+optimises the phase map (optimize_model, go.py:296-336) and reports a loss;
+NNI's annealer proposes the next placement (physical_exp_nni_main.py:11-24).
+
+Here a trial is `PlacementStudy.evaluate`: the same three traces on the GPU,
+a phase-map optimisation on the CUDA objective, and the coverage gain (dB,
+with the optimised metasurface minus without) pooled to a coarse map.  The
+surrogate MLP (surrogate.py) learns descriptor -> gain map from such trials;
+`screened_anneal` lets it rank annealing candidates so that the tracer only
+judges the best few.
+"""
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import objective, scenes, tracer
+
+N_PARAMS = 8
+N_OCC = 64
+
+
+class PlacementStudy:
+    """A seeded room with an AP and an Rx grid; placements on 3 walls."""
+
+    def __init__(self, seed=0, rx=(64, 64), launch=250, max_reflection=2, pool=4,
+                 opt_steps=30, n_boxes=12, sizes=(8, 24)):
+        self.seed = seed
+        self.lam = scenes.WAVE_LEN_60GHZ
+        self.room = (12.0, 8.0, 3.0)
+        self.ap_pos = (6.0, 0.5, 2.5)
+        self.tris, self.mat, self.mat_prop = scenes.shoebox_scene(
+            n_boxes, room=self.room, box_tess=1, seed=seed, keep_clear=[self.ap_pos])
+        self.src = scenes.ula(self.ap_pos, (1, 0, 0), 16, self.lam / 2)
+        self.dst = scenes.rx_grid(0.25, 11.75, rx[0], 0.25, 7.75, rx[1], 1.5)
+        self.rx = rx
+        self.pool = pool
+        self.launch = launch
+        self.L = max_reflection
+        self.opt_steps = opt_steps
+        self.sizes = sizes
+        # walls: (origin of the u axis, u direction, inward normal, length)
+        X, Y, Z = self.room
+        self.walls = [
+            (np.array([0.0, Y, 0.0]), np.array([1.0, 0.0, 0.0]), np.array([0.0, -1.0, 0.0]), X),
+            (np.array([0.0, 0.0, 0.0]), np.array([0.0, 1.0, 0.0]), np.array([1.0, 0.0, 0.0]), Y),
+            (np.array([X, 0.0, 0.0]), np.array([0.0, 1.0, 0.0]), np.array([-1.0, 0.0, 0.0]), Y),
+        ]
+        self.occupancy = self._occupancy()
+        wv = np.ones(16, np.complex64) / 4.0
+        self.W = torch.as_tensor(wv[None], device="cuda")
+        self.scene = tracer.Scene(self.tris, self.mat, self.mat_prop)
+        H0, _ = self._trace(self.scene, self.src, self.dst, 2, 0, (0, 1, 0), (0, 0, 0))
+        self.db0 = self._coverage(H0)
+
+    # ------------------------------------------------------------ helpers
+    def _occupancy(self):
+        X, Y, _ = self.room
+        occ = np.zeros((8, 8))
+        t = self.tris.reshape(-1, 3, 3)
+        lo = t.min(1)
+        hi = t.max(1)
+        boxes = self.mat >= 3
+        for i in range(8):
+            for j in range(8):
+                cx0, cx1 = i * X / 8, (i + 1) * X / 8
+                cy0, cy1 = j * Y / 8, (j + 1) * Y / 8
+                ox = np.clip(np.minimum(hi[boxes, 0], cx1) - np.maximum(lo[boxes, 0], cx0), 0, None)
+                oy = np.clip(np.minimum(hi[boxes, 1], cy1) - np.maximum(lo[boxes, 1], cy0), 0, None)
+                occ[i, j] = min(1.0, float((ox * oy).sum()) / (X * Y / 64) / 12.0)
+        return occ.reshape(-1).astype(np.float32)
+
+    def _params(self, launch):
+        return tracer.make_params(launch, launch, self.lam, self.L, 100)
+
+    def _trace(self, scene, src, dst, sbp, dbp, sdir, ddir):
+        p = tracer.make_params(self.launch, self.launch, self.lam, self.L, 100, sbp, dbp, 5,
+                               0.5e-5, 0.06, sdir, ddir)
+        res, st = scene.trace(src, dst, p)
+        return torch.complex(res[..., 0], res[..., 1]), st
+
+    def _coverage(self, H):
+        y = (self.W @ H).abs()[0]
+        db = 20 * torch.log10(y + 1e-12)
+        n0, n1 = self.rx
+        g = db.reshape(n0 // self.pool, self.pool, n1 // self.pool, self.pool).mean((1, 3))
+        return g.reshape(-1)
+
+    def ms_geometry(self, p):
+        """p = (wall, u, v, size): wall index, position along the wall and
+        height as fractions, side length in elements (lambda/2 pitch)."""
+        wall, u, v, n = int(p[0]), float(p[1]), float(p[2]), int(p[3])
+        org, ud, nrm, length = self.walls[wall]
+        up = np.array([0.0, 0.0, 1.0])
+        center = org + ud * (u * length) + up * (0.3 + v * 2.4) + nrm * 1e-3
+        pitch = self.lam / 2
+        k = np.arange(n) - (n - 1) / 2
+        side = np.cross(nrm, up)
+        pos = (center[None, None, :] - k[:, None, None] * pitch * up[None, None, :]
+               + k[None, :, None] * pitch * side[None, None, :]).astype(np.float32)
+        h = n / 2 * pitch + 1e-3
+        c = center - nrm * 5e-4
+        a, b = up * h, side * h
+        quad = np.array([[c - a - b, c - a + b, c + a - b], [c + a - b, c + a + b, c - a + b]],
+                        np.float32)
+        return pos, quad, nrm.astype(np.float32)
+
+    def descriptor(self, p):
+        wall, u, v, n = int(p[0]), float(p[1]), float(p[2]), int(p[3])
+        lo, hi = self.sizes
+        d = np.zeros(N_PARAMS, np.float32)
+        d[wall] = 1.0
+        d[3], d[4] = u, v
+        d[5] = (n - lo) / max(1, hi - lo)
+        d[6], d[7] = math.sin(math.pi * u), math.cos(math.pi * u)
+        return np.concatenate([d, self.occupancy])
+
+    def random_params(self, rng):
+        lo, hi = self.sizes
+        return (int(rng.integers(0, 3)), float(rng.uniform(0.1, 0.9)), float(rng.uniform(0.1, 0.9)),
+                int(rng.integers(lo // 8, hi // 8 + 1) * 8))
+
+    # ---------------------------------------------------------- one trial
+    def evaluate(self, p, return_detail=False):
+        """Ray-trace + optimise one placement; returns the pooled gain map (dB)."""
+        pos, quad, nrm = self.ms_geometry(p)
+        tris = np.concatenate([self.tris, quad], 0)
+        mat = np.concatenate([self.mat, np.full(2, self.mat_prop.shape[0], np.int32)])
+        mp = np.concatenate([self.mat_prop, np.zeros((1, 19), np.float32)], 0)  # blackhole
+        sc = tracer.Scene(tris, mat, mp)
+        Hd, _ = self._trace(sc, self.src, self.dst, 2, 0, (0, 1, 0), (0, 0, 0))
+        sc.close()
+        Ha, _ = self._trace(self.scene, self.src, pos, 2, 1, (0, 1, 0), nrm)
+        Hr, _ = self._trace(self.scene, pos, self.dst, 1, 0, nrm, (0, 0, 0))
+        M = pos.shape[0] * pos.shape[1]
+        phi = torch.zeros(M, device="cuda", requires_grad=True)
+        opt = torch.optim.Adam([phi], lr=0.3)
+        R = Hd.shape[1]
+        for _ in range(self.opt_steps):
+            loss = objective.capacity_objective(self.W, Hd, Ha, Hr, phi, 2 * math.pi, 1.0 / R)
+            loss.backward()
+            opt.step()
+            opt.zero_grad()
+        with torch.no_grad():
+            H = Hd + (Ha * torch.exp(1j * phi)[None, :]) @ Hr
+            gain = self._coverage(H) - self.db0
+        if return_detail:
+            return gain, dict(H=H, phi=phi.detach())
+        return gain
+
+    def dataset(self, n, seed=0, log=None):
+        rng = np.random.Generator(np.random.PCG64(seed))
+        X, Y, P = [], [], []
+        t0 = time.time()
+        for i in range(n):
+            p = self.random_params(rng)
+            X.append(self.descriptor(p))
+            Y.append(self.evaluate(p).float().cpu().numpy())
+            P.append(p)
+            if log and (i + 1) % 100 == 0:
+                log(f"{i + 1}/{n} samples, {time.time() - t0:.1f}s")
+        return np.stack(X), np.stack(Y), P
+
+
+def score(gain):
+    """Placement figure of merit: mean pooled coverage gain (dB)."""
+    return gain.mean(-1)
+
+
+def anneal_candidates(study, n, rng, surrogate=None, t0=1.0, t1=0.02):
+    """Simulated-annealing chain over placements.  With a surrogate, moves are
+    accepted on its predicted score; every visited placement is returned."""
+    cur = study.random_params(rng)
+    visited = [cur]
+    cur_s = None
+    batch = 256
+    props = []
+    while len(visited) < n:
+        # propose a batch of neighbours, score them together
+        props = []
+        for _ in range(batch):
+            w, u, v, s = cur
+            if rng.random() < 0.1:
+                w = int(rng.integers(0, 3))
+            u = float(np.clip(u + rng.normal(0, 0.08), 0.1, 0.9))
+            v = float(np.clip(v + rng.normal(0, 0.08), 0.1, 0.9))
+            if rng.random() < 0.2:
+                lo, hi = study.sizes
+                s = int(np.clip(s + 8 * rng.choice([-1, 1]), lo, hi))
+            props.append((w, u, v, s))
+        if surrogate is not None:
+            X = torch.as_tensor(np.stack([study.descriptor(q) for q in props]), device="cuda")
+            sc = score(surrogate(X)).cpu().numpy()
+        else:
+            sc = rng.normal(size=len(props))
+        for q, s_ in zip(props, sc):
+            T = t0 * (t1 / t0) ** (len(visited) / n)
+            if cur_s is None or s_ > cur_s or rng.random() < math.exp((s_ - cur_s) / T):
+                cur, cur_s = q, s_
+            visited.append(q)
+            if len(visited) >= n:
+                break
+    return visited[:n]
+
+
+def screening_report(study, mlp, pool_params, pool_gain, top_frac=0.05, t_trial=None,
+                     mlp_batch=4096):
+    """Compare surrogate screening with the plain loop on a traced pool.
+
+    pool_params / pool_gain: placements and their traced gain maps (the plain
+    loop's answer).  The surrogate ranks the whole pool, the tracer judges the
+    top `top_frac`; the pick is compared with the pool's true best.  Rates:
+    plain = 1 / t_trial configs/s; screened = n / (t_rank + k t_trial)."""
+    n = len(pool_params)
+    k = max(1, int(round(top_frac * n)))
+    X = torch.as_tensor(np.stack([study.descriptor(p) for p in pool_params]), device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pred = mlp(X)
+    torch.cuda.synchronize()
+    t_rank = time.perf_counter() - t0
+    ps = score(pred).cpu().numpy()
+    true = score(torch.as_tensor(pool_gain)).numpy()
+    top = np.argsort(-ps)[:k]
+    pick = top[np.argmax(true[top])]
+    if t_trial is None:
+        t0 = time.perf_counter()
+        study.evaluate(pool_params[0])
+        torch.cuda.synchronize()
+        t_trial = time.perf_counter() - t0
+    err = np.abs(pred.cpu().numpy() - pool_gain)
+    return {
+        "pool": n, "judged": k,
+        "surrogate_median_abs_err_db": float(np.median(err)),
+        "mean_predictor_median_abs_err_db": float(np.median(np.abs(pool_gain - pool_gain.mean(0)))),
+        "best_true_score_db": float(true.max()), "screened_pick_score_db": float(true[pick]),
+        "selection_gap_db": float(true.max() - true[pick]),
+        "pick_median_cell_err_db": float(np.median(np.abs(pool_gain[pick] - pool_gain[np.argmax(true)]))),
+        "t_trial_s": t_trial, "t_rank_s": t_rank,
+        "plain_configs_per_s": 1.0 / t_trial,
+        "screened_configs_per_s": n / (t_rank + k * t_trial),
+    }
