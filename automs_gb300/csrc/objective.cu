@@ -18,6 +18,7 @@
 // the second pass reads it from L2, so one evaluation moves H_r from HBM
 // once.  Scratch lives in a per-device buffer kept across calls; calls on
 // one device must not overlap.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -451,6 +452,417 @@ cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *U, float *Yp
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------
+// Single-pass streaming path (one HBM read of H_r and H_d).
+//
+// A persistent CTA per SM walks column tiles of TR Rx.  For each tile the
+// TMA engine copies the (M + S) x TR complex block of [H_r; H_d] into a
+// 2-stage shared-memory ring (cp.async.bulk.tensor, mbarrier completion);
+// the CTA then (A) forms Y for the TR columns, (B) evaluates the per-Rx
+// capacity, max and mask and the two gradient parts, and (C) accumulates
+// P1[c,k] += sum_col G1[c,col] conj(H[k,col]) (and P2 for the norm term)
+// from the same shared-memory tile.  The per-CTA P1/P2 and loss partials are
+// reduced by k_stream_reduce; k_final then forms dphi and dL/dW.
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+  unsigned long long t0 = 0;
+  for (uint32_t it = 0;; it++) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    if (it == 0) t0 = t;
+    else if (t - t0 > 2000000000ull) return false;  // 2 s
+  }
+}
+
+template <int CB, int TR, int KPT>
+__global__ void __launch_bounds__(512, 1)
+    k_obj_stream(ObjArgs a, const __grid_constant__ CUtensorMap mapR,
+                 const __grid_constant__ CUtensorMap mapD, int M, int Mbox, int Mp, int boxR,
+                 int stage_bytes, int ntiles, const float *U, float *Ppart, double *lpart,
+                 unsigned *err) {
+  constexpr int NTH = 512, NW = NTH / 32;
+  const int K = M + a.S;
+  // H_r rows [0, Mbox) come from boxes of boxR rows, H_d rows start at Mp
+  // (a multiple of 16, so every TMA destination is 128-byte aligned)
+  const uint32_t tx_bytes = (uint32_t)(Mbox + a.S) * TR * 8;
+  extern __shared__ unsigned char smem_dyn[];
+  unsigned char *base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
+  c2 *coef = reinterpret_cast<c2 *>(base + 2 * (size_t)stage_bytes);   // [K][CB]
+  __shared__ c2 red[NW][TR][CB];
+  __shared__ c2 g1s[CB][TR], g2s[CB][TR];
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ int abort_flag;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[0])), "r"(1));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[1])), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+  }
+  for (int i = t; i < K * CB; i += NTH) {
+    const int k = i / CB, c = i % CB;
+    c2 v = {0.f, 0.f};
+    if (c < a.C) v = k < M ? ld2(U, (size_t)c * M + k) : ld2(a.W, (size_t)c * a.S + (k - M));
+    coef[i] = v;
+  }
+  __syncthreads();
+
+  auto issue = [&](int tile, int stage) {
+    float2 *dst = reinterpret_cast<float2 *>(base + (size_t)stage * stage_bytes);
+    uint64_t *bar = &full[stage];
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(tx_bytes)
+                 : "memory");
+    const int x = tile * TR * 2;
+    for (int m0 = 0; m0 < Mbox; m0 += boxR)
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+          " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst + (size_t)m0 * TR)),
+          "l"(reinterpret_cast<uint64_t>(&mapR)), "r"(x), "r"(m0), "r"(smem_addr(bar))
+          : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_addr(dst + (size_t)Mp * TR)),
+        "l"(reinterpret_cast<uint64_t>(&mapD)), "r"(x), "r"(0), "r"(smem_addr(bar))
+        : "memory");
+  };
+  const int first = blockIdx.x;
+  if (t == 0) {
+    if (first < ntiles) issue(first, 0);
+    if (first + (int)gridDim.x < ntiles) issue(first + gridDim.x, 1);
+  }
+
+  c2 p1[KPT][CB], p2[KPT][CB];
+#pragma unroll
+  for (int q = 0; q < KPT; q++)
+#pragma unroll
+    for (int c = 0; c < CB; c++) { p1[q][c] = {0.f, 0.f}; p2[q][c] = {0.f, 0.f}; }
+  double sum_max = 0.0, sum_sq = 0.0;
+  const int col = t % TR, j = t / TR;
+  constexpr int NJ = NTH / TR;
+
+  int it = 0;
+  for (int tile = first; tile < ntiles; tile += gridDim.x, it++) {
+    const int stg = it & 1;
+    if (!mbar_wait_bounded(&full[stg], (it >> 1) & 1)) {
+      if (t == 0) atomicOr(err, 1u);
+      abort_flag = 1;
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    const float2 *T = reinterpret_cast<const float2 *>(base + (size_t)stg * stage_bytes);
+    // (A) Y for the tile's columns; lanes with equal col are TR apart
+    c2 y[CB];
+#pragma unroll
+    for (int c = 0; c < CB; c++) y[c] = {0.f, 0.f};
+    for (int k = j; k < K; k += NJ) {
+      const int row = k < M ? k : Mp + (k - M);
+      const float2 h = T[(size_t)row * TR + col];
+#pragma unroll
+      for (int c = 0; c < CB; c++) mac(y[c], coef[(size_t)k * CB + c], c2{h.x, h.y});
+    }
+#pragma unroll
+    for (int c = 0; c < CB; c++)
+      for (int o = TR; o < 32; o <<= 1) {
+        y[c].x += __shfl_xor_sync(0xffffffffu, y[c].x, o);
+        y[c].y += __shfl_xor_sync(0xffffffffu, y[c].y, o);
+      }
+    if (lane < TR)
+#pragma unroll
+      for (int c = 0; c < CB; c++) red[warp][lane][c] = y[c];
+    __syncthreads();
+    // (B) per-Rx capacity, max, mask, gradient parts
+    if (t < TR) {
+      const int r = tile * TR + t;
+      c2 yy[CB];
+      float cap[CB], amp[CB];
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        c2 acc = {0.f, 0.f};
+#pragma unroll
+        for (int w = 0; w < NW; w++) { acc.x += red[w][t][c].x; acc.y += red[w][t][c].y; }
+        yy[c] = acc;
+      }
+      int arg = 0;
+      float mx = -1.f;
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        if (c >= a.C) { cap[c] = 0.f; amp[c] = 0.f; continue; }
+        amp[c] = sqrtf(yy[c].x * yy[c].x + yy[c].y * yy[c].y);
+        const float aa = amp[c] + kEps;
+        float v = log2f(1.0f + aa * aa / kN0);
+        if (a.drop && a.drop[c]) v = 0.f;
+        cap[c] = v;
+        if (v > mx) { mx = v; arg = c; }
+        if (a.recv_amp && r < a.R) a.recv_amp[(size_t)c * a.R + r] = amp[c];
+      }
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        c2 ga = {0.f, 0.f}, gb = {0.f, 0.f};
+        if (c < a.C && r < a.R) {
+          const bool dropped = a.drop && a.drop[c];
+          const float msk = (cap[c] != mx) ? cap[c] : 0.f;
+          sum_sq += (double)msk * msk;
+          const float aa = amp[c] + kEps;
+          const float dcap = (2.0f * aa / kN0) / (1.0f + aa * aa / kN0) * kInvLn2;
+          float g1 = (c == arg) ? -a.w : 0.f, g2 = msk;
+          if (dropped) { g1 = 0.f; g2 = 0.f; }
+          const float sc = amp[c] > 0.f ? dcap / amp[c] : 0.f;
+          ga = {g1 * sc * yy[c].x, g1 * sc * yy[c].y};
+          gb = {g2 * sc * yy[c].x, g2 * sc * yy[c].y};
+        }
+        g1s[c][t] = ga;
+        g2s[c][t] = gb;
+      }
+      if (r < a.R) sum_max += mx;
+    }
+    __syncthreads();
+    // (C) P += G conj(H) over the tile's columns, rows k = t + NTH q
+#pragma unroll
+    for (int q = 0; q < KPT; q++) {
+      const int k = t + NTH * q;
+      if (k < K) {
+        const int row = k < M ? k : Mp + (k - M);
+        const float2 *hr = T + (size_t)row * TR;
+#pragma unroll
+        for (int cc = 0; cc < TR; cc++) {
+          const float2 h = hr[cc];
+#pragma unroll
+          for (int c = 0; c < CB; c++) {
+            macc(p1[q][c], g1s[c][cc], c2{h.x, h.y});
+            if (CB > 1) macc(p2[q][c], g2s[c][cc], c2{h.x, h.y});
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // the stage is free: order the generic reads before the async-proxy refill
+    if (t == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (tile + 2 * (int)gridDim.x < ntiles) issue(tile + 2 * gridDim.x, stg);
+    }
+  }
+  // partials of this CTA: P1 at [b][c][k], P2 at [b][C + c][k]
+#pragma unroll
+  for (int q = 0; q < KPT; q++) {
+    const int k = t + NTH * q;
+    if (k >= K) continue;
+#pragma unroll
+    for (int c = 0; c < CB; c++) {
+      if (c >= a.C) continue;
+      float2 *o = reinterpret_cast<float2 *>(Ppart) + ((size_t)blockIdx.x * 2 * a.C + c) * K + k;
+      o[0] = make_float2(p1[q][c].x, p1[q][c].y);
+      o[(size_t)a.C * K] = make_float2(p2[q][c].x, p2[q][c].y);
+    }
+  }
+  if (t < 32) {
+    for (int o = 16; o > 0; o >>= 1) {
+      sum_max += __shfl_xor_sync(0xffffffffu, sum_max, o);
+      sum_sq += __shfl_xor_sync(0xffffffffu, sum_sq, o);
+    }
+    if (t == 0) {
+      lpart[2 * blockIdx.x] = sum_max;
+      lpart[2 * blockIdx.x + 1] = sum_sq;
+    }
+  }
+}
+
+// reduce the CTA partials: GU[c,k] = sum_b P1 + (sum_b P2) / ||masked||;
+// 4 threads per element; block 0 also writes the loss.
+__global__ void __launch_bounds__(256) k_stream_reduce(ObjArgs a, int K, int nb,
+                                                       const float *Ppart, const double *lpart,
+                                                       float *GU) {
+  __shared__ float inv_s;
+  if (threadIdx.x < 32) {
+    double x = 0, z = 0;
+    for (int b = threadIdx.x; b < nb; b += 32) { x += lpart[2 * b]; z += lpart[2 * b + 1]; }
+    for (int o = 16; o > 0; o >>= 1) {
+      x += __shfl_xor_sync(0xffffffffu, x, o);
+      z += __shfl_xor_sync(0xffffffffu, z, o);
+    }
+    if (threadIdx.x == 0) {
+      const double nrm = sqrt(z);
+      inv_s = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+      if (blockIdx.x == 0 && a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
+    }
+  }
+  __syncthreads();
+  const long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int sub = threadIdx.x & 3;
+  const long long n = (long long)a.C * K;
+  if (e >= n) return;
+  const int c = (int)(e / K), k = (int)(e % K);
+  c2 s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
+  const float2 *P = reinterpret_cast<const float2 *>(Ppart);
+#pragma unroll 4
+  for (int b = sub; b < nb; b += 4) {
+    const float2 u = P[((size_t)b * 2 * a.C + c) * K + k];
+    const float2 v = P[((size_t)b * 2 * a.C + a.C + c) * K + k];
+    s1.x += u.x; s1.y += u.y;
+    s2.x += v.x; s2.y += v.y;
+  }
+  for (int o = 1; o < 4; o <<= 1) {
+    s1.x += __shfl_xor_sync(0xffffffffu, s1.x, o);
+    s1.y += __shfl_xor_sync(0xffffffffu, s1.y, o);
+    s2.x += __shfl_xor_sync(0xffffffffu, s2.x, o);
+    s2.y += __shfl_xor_sync(0xffffffffu, s2.y, o);
+  }
+  if (sub == 0)
+    reinterpret_cast<float2 *>(GU)[e] = make_float2(fmaf(s2.x, inv_s, s1.x), fmaf(s2.y, inv_s, s1.y));
+}
+
+using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                              const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                              const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                              CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeFn tmap_encoder() {
+  static EncodeFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeFn>(p);
+  }
+  return fn;
+}
+
+// complex [rows, R] as a float [rows, 2R] tensor; box (2 TR floats) x box_rows
+bool make_cmap(CUtensorMap *m, const float *base, int rows, int R, int TR, int box_rows) {
+  EncodeFn enc = tmap_encoder();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)2 * R, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)R * 8};
+  cuuint32_t box[2] = {(cuuint32_t)(2 * TR), (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box,
+             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+struct StreamPlan {
+  bool ok = false;
+  int TR = 0, KPT = 0, Mbox = 0, Mp = 0, boxR = 0, stage_bytes = 0, ntiles = 0, grid = 0;
+  size_t smem = 0;
+};
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+// the single-pass path needs the whole [H_r; H_d] column tile in shared memory
+StreamPlan stream_plan(int S, int M, int R, int C, bool grad_y) {
+  StreamPlan p;
+  const int CB = cbucket(C);
+  if (grad_y || CB > 2 || R % 2 || S > 256 || M < 0) return p;
+  const int K = M + S;
+  const int kpt = (K + 511) / 512;
+  int KPT = kpt <= 2 ? 2 : (kpt <= 4 ? 4 : (kpt <= 8 ? 8 : 0));
+  if (!KPT || (CB == 2 && KPT > 4)) return p;
+  p.boxR = M <= 256 ? std::max(M, 1) : 256;
+  p.Mbox = M <= 0 ? 0 : (M + p.boxR - 1) / p.boxR * p.boxR;
+  p.Mp = (p.Mbox + 15) / 16 * 16;
+  for (int TR : {8, 4, 2}) {
+    const size_t stage = ((size_t)(p.Mp + S) * TR * 8 + 1023) / 1024 * 1024;
+    const size_t smem = 1024 + 2 * stage + (size_t)K * CB * 8;
+    if (smem <= 200 * 1024) {
+      p.TR = TR;
+      p.stage_bytes = (int)stage;
+      p.smem = smem;
+      break;
+    }
+  }
+  if (!p.TR) return p;
+  p.KPT = KPT;
+  p.ntiles = (R + p.TR - 1) / p.TR;
+  p.grid = std::min(sm_count(), p.ntiles);
+  p.ok = true;
+  return p;
+}
+
+template <int CB, int TR, int KPT>
+cudaError_t launch_stream_t(const ObjArgs &a, const StreamPlan &pl, const CUtensorMap &mr,
+                            const CUtensorMap &md, int M, const float *U, float *Ppart,
+                            double *lpart, unsigned *err, cudaStream_t st) {
+  auto kfn = k_obj_stream<CB, TR, KPT>;
+  static size_t set_bytes = 0;
+  if (set_bytes < pl.smem) {
+    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)pl.smem);
+    if (e != cudaSuccess) return e;
+    set_bytes = pl.smem;
+  }
+  kfn<<<pl.grid, 512, pl.smem, st>>>(a, mr, md, M, pl.Mbox, pl.Mp, pl.boxR, pl.stage_bytes,
+                                      pl.ntiles, U, Ppart, lpart, err);
+  return cudaGetLastError();
+}
+
+template <int CB, int TR>
+cudaError_t launch_stream_k(const ObjArgs &a, const StreamPlan &pl, const CUtensorMap &mr,
+                            const CUtensorMap &md, int M, const float *U, float *Ppart,
+                            double *lpart, unsigned *err, cudaStream_t st) {
+  switch (pl.KPT) {
+    case 2: return launch_stream_t<CB, TR, 2>(a, pl, mr, md, M, U, Ppart, lpart, err, st);
+    case 4: return launch_stream_t<CB, TR, 4>(a, pl, mr, md, M, U, Ppart, lpart, err, st);
+    case 8:
+      if (CB == 1) return launch_stream_t<1, TR, 8>(a, pl, mr, md, M, U, Ppart, lpart, err, st);
+      return cudaErrorInvalidValue;
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int CB>
+cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, float *Ppart,
+                       double *lpart, float *GU, float *gw_part, unsigned *counter,
+                       unsigned *err, cudaStream_t st) {
+  CUtensorMap mr, md;
+  const float *Hr = M > 0 ? a.Hr : a.Hd;  // no metasurface: mapR is unused (Mp = 0)
+  if (!make_cmap(&mr, Hr, std::max(M, 1), a.R, pl.TR, pl.boxR) ||
+      !make_cmap(&md, a.Hd, a.S, a.R, pl.TR, a.S))
+    return cudaErrorInvalidValue;
+  if (M > 0) {
+    dim3 gp((M + 127) / 128, a.C);
+    k_prep<<<gp, 128, 0, st>>>(a, M, U);
+  }
+  cudaError_t e;
+  switch (pl.TR) {
+    case 8: e = launch_stream_k<CB, 8>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
+    case 4: e = launch_stream_k<CB, 4>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
+    default: e = launch_stream_k<CB, 2>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
+  }
+  if (e != cudaSuccess) return e;
+  const int K = M + a.S;
+  const long long n = (long long)a.C * K * 4;
+  k_stream_reduce<<<(int)((n + 255) / 256), 256, 0, st>>>(a, K, pl.grid, Ppart, lpart, GU);
+  if (!a.grad_W && !a.grad_phi) return cudaGetLastError();
+  const int nbf = std::max(1, (M + 31) / 32);
+  k_final<CB><<<nbf, 256, 0, st>>>(a, M, K, 1, U, GU, gw_part, counter);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
@@ -466,6 +878,10 @@ ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
   L.G2 = o; o += al(8 * (size_t)C * R);
   L.part = o; o += al(16 * (size_t)sp.nb_epi);
   L.GU = o; o += al(8 * (size_t)sp.rspl * C * sp.K);      // G_U partials
+  const int nsm = 256;                                    // CTA partials of the streaming path
+  L.Pp = o; o += al(8 * (size_t)nsm * 2 * C * sp.K);
+  L.lp = o; o += al(16 * (size_t)nsm);
+  L.GUs = o; o += al(8 * (size_t)C * sp.K);
   L.total = o;
   return L;
 }
@@ -486,6 +902,16 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
   unsigned *counter = reinterpret_cast<unsigned *>(scratch + L.inv + 32);
   float *Um = reinterpret_cast<float *>(scratch + L.Um);
   float *gw = reinterpret_cast<float *>(scratch + L.gw);
+  const StreamPlan pl = stream_plan(a.S, M, a.R, a.C, a.grad_Y != nullptr);
+  if (pl.ok && pl.grid <= 256 &&
+      !((reinterpret_cast<uintptr_t>(a.Hd) | reinterpret_cast<uintptr_t>(ms ? a.Hr : a.Hd)) & 15)) {
+    float *Pp = reinterpret_cast<float *>(scratch + L.Pp);
+    double *lp = reinterpret_cast<double *>(scratch + L.lp);
+    float *GUs = reinterpret_cast<float *>(scratch + L.GUs);
+    unsigned *err = reinterpret_cast<unsigned *>(scratch + L.inv + 48);
+    if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Um, Pp, lp, GUs, gw, counter + 1, err, st);
+    return run_stream<2>(a, pl, M, Um, Pp, lp, GUs, gw, counter + 1, err, st);
+  }
   switch (cbucket(a.C)) {
 #define CASE(CB) case CB: return run_cb<CB>(a, sp, M, Um, Ypart, G1, G2, part, counter, scal, GUp, gw, st);
     CASE(1) CASE(2) CASE(4) CASE(8) CASE(16) CASE(32) CASE(64)
