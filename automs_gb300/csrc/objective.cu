@@ -487,12 +487,11 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 }
 
 template <int CB, int TR, int KPT>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(256, 2)
     k_obj_stream(ObjArgs a, const __grid_constant__ CUtensorMap mapR,
                  const __grid_constant__ CUtensorMap mapD, int M, int Mbox, int Mp, int boxR,
-                 int stage_bytes, int ntiles, const float *U, float *Ppart, double *lpart,
-                 unsigned *err) {
-  constexpr int NTH = 512, NW = NTH / 32;
+                 int stage_bytes, int ntiles, float *Ppart, double *lpart, unsigned *err) {
+  constexpr int NTH = 256, NW = NTH / 32;
   const int K = M + a.S;
   // H_r rows [0, Mbox) come from boxes of boxR rows, H_d rows start at Mp
   // (a multiple of 16, so every TMA destination is 128-byte aligned)
@@ -506,20 +505,6 @@ __global__ void __launch_bounds__(512, 1)
   __shared__ __align__(8) uint64_t full[2];
   __shared__ int abort_flag;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-
-  if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[0])), "r"(1));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[1])), "r"(1));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    abort_flag = 0;
-  }
-  for (int i = t; i < K * CB; i += NTH) {
-    const int k = i / CB, c = i % CB;
-    c2 v = {0.f, 0.f};
-    if (c < a.C) v = k < M ? ld2(U, (size_t)c * M + k) : ld2(a.W, (size_t)c * a.S + (k - M));
-    coef[i] = v;
-  }
-  __syncthreads();
 
   auto issue = [&](int tile, int stage) {
     float2 *dst = reinterpret_cast<float2 *>(base + (size_t)stage * stage_bytes);
@@ -542,9 +527,44 @@ __global__ void __launch_bounds__(512, 1)
   };
   const int first = blockIdx.x;
   if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[0])), "r"(1));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[1])), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
     if (first < ntiles) issue(first, 0);
     if (first + (int)gridDim.x < ntiles) issue(first + gridDim.x, 1);
   }
+  // coefficients while the first tiles are in flight: U = (W H_a) e^{j phi'}
+  // for metasurface rows, W for the H_d rows
+  for (int i = t; i < K * CB; i += NTH) {
+    const int k = i / CB, c = i % CB;
+    c2 v = {0.f, 0.f};
+    if (c < a.C) {
+      if (k < M) {
+        c2 acc = {0.f, 0.f};
+        int s2 = 0;
+        for (; s2 + 8 <= a.S; s2 += 8) {
+          c2 h[8], w[8];
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            h[q] = ld2(a.Ha, (size_t)(s2 + q) * M + k);
+            w[q] = ld2(a.W, (size_t)c * a.S + s2 + q);
+          }
+#pragma unroll
+          for (int q = 0; q < 8; q++) mac(acc, w[q], h[q]);
+        }
+        for (; s2 < a.S; s2++) mac(acc, ld2(a.W, (size_t)c * a.S + s2), ld2(a.Ha, (size_t)s2 * M + k));
+        const float pp = py_mod(__ldg(a.phi + k), a.max_phase);
+        float sn, cs;
+        sincosf(pp, &sn, &cs);
+        mac(v, acc, c2{cs, sn});
+      } else {
+        v = ld2(a.W, (size_t)c * a.S + (k - M));
+      }
+    }
+    coef[i] = v;
+  }
+  __syncthreads();
 
   c2 p1[KPT][CB], p2[KPT][CB];
 #pragma unroll
@@ -569,6 +589,7 @@ __global__ void __launch_bounds__(512, 1)
     c2 y[CB];
 #pragma unroll
     for (int c = 0; c < CB; c++) y[c] = {0.f, 0.f};
+#pragma unroll 4
     for (int k = j; k < K; k += NJ) {
       const int row = k < M ? k : Mp + (k - M);
       const float2 h = T[(size_t)row * TR + col];
@@ -631,7 +652,8 @@ __global__ void __launch_bounds__(512, 1)
       if (r < a.R) sum_max += mx;
     }
     __syncthreads();
-    // (C) P += G conj(H) over the tile's columns, rows k = t + NTH q
+    // (C) P += G conj(H) over the tile's columns, rows k = t + NTH q; the
+    // column order is rotated by the lane so a warp's reads spread over banks
 #pragma unroll
     for (int q = 0; q < KPT; q++) {
       const int k = t + NTH * q;
@@ -639,7 +661,8 @@ __global__ void __launch_bounds__(512, 1)
         const int row = k < M ? k : Mp + (k - M);
         const float2 *hr = T + (size_t)row * TR;
 #pragma unroll
-        for (int cc = 0; cc < TR; cc++) {
+        for (int cc0 = 0; cc0 < TR; cc0++) {
+          const int cc = (cc0 + lane) & (TR - 1);
           const float2 h = hr[cc];
 #pragma unroll
           for (int c = 0; c < CB; c++) {
@@ -666,7 +689,7 @@ __global__ void __launch_bounds__(512, 1)
       if (c >= a.C) continue;
       float2 *o = reinterpret_cast<float2 *>(Ppart) + ((size_t)blockIdx.x * 2 * a.C + c) * K + k;
       o[0] = make_float2(p1[q][c].x, p1[q][c].y);
-      o[(size_t)a.C * K] = make_float2(p2[q][c].x, p2[q][c].y);
+      if (CB > 1) o[(size_t)a.C * K] = make_float2(p2[q][c].x, p2[q][c].y);
     }
   }
   if (t < 32) {
@@ -681,48 +704,131 @@ __global__ void __launch_bounds__(512, 1)
   }
 }
 
-// reduce the CTA partials: GU[c,k] = sum_b P1 + (sum_b P2) / ||masked||;
-// 4 threads per element; block 0 also writes the loss.
-__global__ void __launch_bounds__(256) k_stream_reduce(ObjArgs a, int K, int nb,
-                                                       const float *Ppart, const double *lpart,
-                                                       float *GU) {
+// final of the streaming path.  Each CTA owns 32 metasurface rows: it reduces
+// their CTA partials G_U = sum P1 + (sum P2) / ||masked||, writes
+// dphi = -sum_c Im(conj(G_U) U) and partial sums of dL/dW; the last CTA adds
+// those and the H_d rows into grad_W.  Block 0 writes the loss.
+template <int CB>
+__global__ void __launch_bounds__(256) k_stream_final(ObjArgs a, int M, int nparts,
+                                                      const float *Ppart, const double *lpart,
+                                                      float *gw_part, unsigned *counter) {
+  __shared__ c2 gu[CB][32];
+  __shared__ c2 ph[32];
   __shared__ float inv_s;
-  if (threadIdx.x < 32) {
+  __shared__ bool last;
+  const int t = threadIdx.x, lane = t & 31;
+  const int K = M + a.S;
+  const int m0 = blockIdx.x * 32;
+  const int nm = max(0, min(32, M - m0));
+  const float2 *P = reinterpret_cast<const float2 *>(Ppart);
+  if (t < 32) {
     double x = 0, z = 0;
-    for (int b = threadIdx.x; b < nb; b += 32) { x += lpart[2 * b]; z += lpart[2 * b + 1]; }
+    for (int b = t; b < nparts; b += 32) { x += lpart[2 * b]; z += lpart[2 * b + 1]; }
     for (int o = 16; o > 0; o >>= 1) {
       x += __shfl_xor_sync(0xffffffffu, x, o);
       z += __shfl_xor_sync(0xffffffffu, z, o);
     }
-    if (threadIdx.x == 0) {
+    if (t == 0) {
       const double nrm = sqrt(z);
       inv_s = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
       if (blockIdx.x == 0 && a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
     }
+    c2 e = {0.f, 0.f};
+    if (t < nm) {
+      const float pp = py_mod(__ldg(a.phi + m0 + t), a.max_phase);
+      sincosf(pp, &e.y, &e.x);
+    }
+    ph[t] = e;
   }
   __syncthreads();
-  const long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
-  const int sub = threadIdx.x & 3;
-  const long long n = (long long)a.C * K;
-  if (e >= n) return;
-  const int c = (int)(e / K), k = (int)(e % K);
-  c2 s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
-  const float2 *P = reinterpret_cast<const float2 *>(Ppart);
+  const float inv = inv_s;
+  // 8 threads per (c, row): each sums every 8th CTA partial
+  for (int e0 = 0; e0 < CB * 32; e0 += 32) {
+    const int e = e0 + (t >> 3), sub = t & 7;
+    const int c = e / 32, jj = e % 32;
+    c2 s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
+    if (c < a.C && jj < nm) {
 #pragma unroll 4
-  for (int b = sub; b < nb; b += 4) {
-    const float2 u = P[((size_t)b * 2 * a.C + c) * K + k];
-    const float2 v = P[((size_t)b * 2 * a.C + a.C + c) * K + k];
-    s1.x += u.x; s1.y += u.y;
-    s2.x += v.x; s2.y += v.y;
+      for (int b = sub; b < nparts; b += 8) {
+        const float2 u = __ldcg(P + ((size_t)b * 2 * a.C + c) * K + m0 + jj);
+        s1.x += u.x; s1.y += u.y;
+        if (CB > 1) {
+          const float2 v = __ldcg(P + ((size_t)b * 2 * a.C + a.C + c) * K + m0 + jj);
+          s2.x += v.x; s2.y += v.y;
+        }
+      }
+    }
+    for (int o = 1; o < 8; o <<= 1) {
+      s1.x += __shfl_xor_sync(0xffffffffu, s1.x, o);
+      s1.y += __shfl_xor_sync(0xffffffffu, s1.y, o);
+      s2.x += __shfl_xor_sync(0xffffffffu, s2.x, o);
+      s2.y += __shfl_xor_sync(0xffffffffu, s2.y, o);
+    }
+    if (sub == 0 && c < CB) gu[c][jj] = c2{fmaf(s2.x, inv, s1.x), fmaf(s2.y, inv, s1.y)};
   }
-  for (int o = 1; o < 4; o <<= 1) {
-    s1.x += __shfl_xor_sync(0xffffffffu, s1.x, o);
-    s1.y += __shfl_xor_sync(0xffffffffu, s1.y, o);
-    s2.x += __shfl_xor_sync(0xffffffffu, s2.x, o);
-    s2.y += __shfl_xor_sync(0xffffffffu, s2.y, o);
+  __syncthreads();
+  if (a.grad_phi) {
+    // dphi[m] = -sum_c Im(conj(G_U) U) with U = (W H_a) e^{j phi'} recomputed,
+    // 8 lanes per row splitting the sum over the AP elements
+    const int jj = t >> 3, sub = t & 7;
+    float sacc = 0.f;
+    for (int c = 0; c < a.C; c++) {
+      c2 acc = {0.f, 0.f};
+      if (jj < nm)
+        for (int s2 = sub; s2 < a.S; s2 += 8)
+          mac(acc, ld2(a.W, (size_t)c * a.S + s2), ld2(a.Ha, (size_t)s2 * M + m0 + jj));
+      for (int o = 1; o < 8; o <<= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      }
+      if (jj < nm) {
+        c2 u = {0.f, 0.f};
+        mac(u, acc, ph[jj]);
+        const c2 g = gu[c][jj];
+        sacc += g.x * u.y - g.y * u.x;  // Im(conj(g) u)
+      }
+    }
+    if (sub == 0 && jj < nm) a.grad_phi[m0 + jj] = -sacc;
   }
-  if (sub == 0)
-    reinterpret_cast<float2 *>(GU)[e] = make_float2(fmaf(s2.x, inv_s, s1.x), fmaf(s2.y, inv_s, s1.y));
+  if (!a.grad_W) return;
+  for (int i = t; i < a.C * a.S; i += blockDim.x) {
+    const int c = i / a.S, s2 = i % a.S;
+    c2 acc = {0.f, 0.f};
+    for (int jj = 0; jj < nm; jj++) {
+      const c2 g = gu[c][jj], e = ph[jj];
+      const c2 gv = {g.x * e.x + g.y * e.y, g.y * e.x - g.x * e.y};  // g e^{-j p}
+      macc(acc, gv, ld2(a.Ha, (size_t)s2 * M + m0 + jj));
+    }
+    reinterpret_cast<float2 *>(gw_part)[(size_t)blockIdx.x * a.C * a.S + i] = make_float2(acc.x, acc.y);
+  }
+  __threadfence();
+  __syncthreads();
+  if (t == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int i = t; i < a.C * a.S; i += blockDim.x) {
+    const int c = i / a.S, s2 = i % a.S;
+    c2 acc = {0.f, 0.f}, a2 = {0.f, 0.f};
+    for (int b = 0; b < nparts; b++) {
+      const float2 u = __ldcg(P + ((size_t)b * 2 * a.C + c) * K + M + s2);
+      acc.x += u.x; acc.y += u.y;
+      if (CB > 1) {
+        const float2 v = __ldcg(P + ((size_t)b * 2 * a.C + a.C + c) * K + M + s2);
+        a2.x += v.x; a2.y += v.y;
+      }
+    }
+    acc.x = fmaf(a2.x, inv, acc.x);
+    acc.y = fmaf(a2.y, inv, acc.y);
+    const float2 *gp = reinterpret_cast<const float2 *>(gw_part);
+#pragma unroll 4
+    for (int b = 0; b < (int)gridDim.x; b++) {
+      const float2 u = __ldcg(gp + (size_t)b * a.C * a.S + i);
+      acc.x += u.x; acc.y += u.y;
+    }
+    reinterpret_cast<float2 *>(a.grad_W)[i] = make_float2(acc.x, acc.y);
+  }
+  if (t == 0) *counter = 0u;  // ready for the next call
 }
 
 using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -779,16 +885,16 @@ StreamPlan stream_plan(int S, int M, int R, int C, bool grad_y) {
   const int CB = cbucket(C);
   if (grad_y || CB > 2 || R % 2 || S > 256 || M < 0) return p;
   const int K = M + S;
-  const int kpt = (K + 511) / 512;
-  int KPT = kpt <= 2 ? 2 : (kpt <= 4 ? 4 : (kpt <= 8 ? 8 : 0));
-  if (!KPT || (CB == 2 && KPT > 4)) return p;
+  const int kpt = (K + 255) / 256;
+  int KPT = kpt <= 4 ? 4 : (kpt <= 8 ? 8 : (kpt <= 16 ? 16 : 0));
+  if (!KPT || (CB == 2 && KPT > 8)) return p;
   p.boxR = M <= 256 ? std::max(M, 1) : 256;
   p.Mbox = M <= 0 ? 0 : (M + p.boxR - 1) / p.boxR * p.boxR;
   p.Mp = (p.Mbox + 15) / 16 * 16;
   for (int TR : {8, 4, 2}) {
     const size_t stage = ((size_t)(p.Mp + S) * TR * 8 + 1023) / 1024 * 1024;
     const size_t smem = 1024 + 2 * stage + (size_t)K * CB * 8;
-    if (smem <= 200 * 1024) {
+    if (smem <= 110 * 1024) {  // two CTAs per SM
       p.TR = TR;
       p.stage_bytes = (int)stage;
       p.smem = smem;
@@ -798,15 +904,15 @@ StreamPlan stream_plan(int S, int M, int R, int C, bool grad_y) {
   if (!p.TR) return p;
   p.KPT = KPT;
   p.ntiles = (R + p.TR - 1) / p.TR;
-  p.grid = std::min(sm_count(), p.ntiles);
+  p.grid = std::min(2 * sm_count(), p.ntiles);
   p.ok = true;
   return p;
 }
 
 template <int CB, int TR, int KPT>
 cudaError_t launch_stream_t(const ObjArgs &a, const StreamPlan &pl, const CUtensorMap &mr,
-                            const CUtensorMap &md, int M, const float *U, float *Ppart,
-                            double *lpart, unsigned *err, cudaStream_t st) {
+                            const CUtensorMap &md, int M, float *Ppart, double *lpart,
+                            unsigned *err, cudaStream_t st) {
   auto kfn = k_obj_stream<CB, TR, KPT>;
   static size_t set_bytes = 0;
   if (set_bytes < pl.smem) {
@@ -815,51 +921,43 @@ cudaError_t launch_stream_t(const ObjArgs &a, const StreamPlan &pl, const CUtens
     if (e != cudaSuccess) return e;
     set_bytes = pl.smem;
   }
-  kfn<<<pl.grid, 512, pl.smem, st>>>(a, mr, md, M, pl.Mbox, pl.Mp, pl.boxR, pl.stage_bytes,
-                                      pl.ntiles, U, Ppart, lpart, err);
+  kfn<<<pl.grid, 256, pl.smem, st>>>(a, mr, md, M, pl.Mbox, pl.Mp, pl.boxR, pl.stage_bytes,
+                                      pl.ntiles, Ppart, lpart, err);
   return cudaGetLastError();
 }
 
 template <int CB, int TR>
 cudaError_t launch_stream_k(const ObjArgs &a, const StreamPlan &pl, const CUtensorMap &mr,
-                            const CUtensorMap &md, int M, const float *U, float *Ppart,
-                            double *lpart, unsigned *err, cudaStream_t st) {
+                            const CUtensorMap &md, int M, float *Ppart, double *lpart,
+                            unsigned *err, cudaStream_t st) {
   switch (pl.KPT) {
-    case 2: return launch_stream_t<CB, TR, 2>(a, pl, mr, md, M, U, Ppart, lpart, err, st);
-    case 4: return launch_stream_t<CB, TR, 4>(a, pl, mr, md, M, U, Ppart, lpart, err, st);
-    case 8:
-      if (CB == 1) return launch_stream_t<1, TR, 8>(a, pl, mr, md, M, U, Ppart, lpart, err, st);
+    case 4: return launch_stream_t<CB, TR, 4>(a, pl, mr, md, M, Ppart, lpart, err, st);
+    case 8: return launch_stream_t<CB, TR, 8>(a, pl, mr, md, M, Ppart, lpart, err, st);
+    case 16:
+      if (CB == 1) return launch_stream_t<1, TR, 16>(a, pl, mr, md, M, Ppart, lpart, err, st);
       return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
   }
 }
 
 template <int CB>
-cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, float *Ppart,
-                       double *lpart, float *GU, float *gw_part, unsigned *counter,
-                       unsigned *err, cudaStream_t st) {
+cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *Ppart,
+                       double *lpart, float *gw_part, unsigned *counter, unsigned *err,
+                       cudaStream_t st) {
   CUtensorMap mr, md;
-  const float *Hr = M > 0 ? a.Hr : a.Hd;  // no metasurface: mapR is unused (Mp = 0)
+  const float *Hr = M > 0 ? a.Hr : a.Hd;  // no metasurface: mapR is unused (Mbox = 0)
   if (!make_cmap(&mr, Hr, std::max(M, 1), a.R, pl.TR, pl.boxR) ||
       !make_cmap(&md, a.Hd, a.S, a.R, pl.TR, a.S))
     return cudaErrorInvalidValue;
-  if (M > 0) {
-    dim3 gp((M + 127) / 128, a.C);
-    k_prep<<<gp, 128, 0, st>>>(a, M, U);
-  }
   cudaError_t e;
   switch (pl.TR) {
-    case 8: e = launch_stream_k<CB, 8>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
-    case 4: e = launch_stream_k<CB, 4>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
-    default: e = launch_stream_k<CB, 2>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
+    case 8: e = launch_stream_k<CB, 8>(a, pl, mr, md, M, Ppart, lpart, err, st); break;
+    case 4: e = launch_stream_k<CB, 4>(a, pl, mr, md, M, Ppart, lpart, err, st); break;
+    default: e = launch_stream_k<CB, 2>(a, pl, mr, md, M, Ppart, lpart, err, st); break;
   }
   if (e != cudaSuccess) return e;
-  const int K = M + a.S;
-  const long long n = (long long)a.C * K * 4;
-  k_stream_reduce<<<(int)((n + 255) / 256), 256, 0, st>>>(a, K, pl.grid, Ppart, lpart, GU);
-  if (!a.grad_W && !a.grad_phi) return cudaGetLastError();
   const int nbf = std::max(1, (M + 31) / 32);
-  k_final<CB><<<nbf, 256, 0, st>>>(a, M, K, 1, U, GU, gw_part, counter);
+  k_stream_final<CB><<<nbf, 256, 0, st>>>(a, M, pl.grid, Ppart, lpart, gw_part, counter);
   return cudaGetLastError();
 }
 
@@ -878,7 +976,7 @@ ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
   L.G2 = o; o += al(8 * (size_t)C * R);
   L.part = o; o += al(16 * (size_t)sp.nb_epi);
   L.GU = o; o += al(8 * (size_t)sp.rspl * C * sp.K);      // G_U partials
-  const int nsm = 256;                                    // CTA partials of the streaming path
+  const int nsm = 512;                                    // CTA partials of the streaming path
   L.Pp = o; o += al(8 * (size_t)nsm * 2 * C * sp.K);
   L.lp = o; o += al(16 * (size_t)nsm);
   L.GUs = o; o += al(8 * (size_t)C * sp.K);
@@ -903,14 +1001,13 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
   float *Um = reinterpret_cast<float *>(scratch + L.Um);
   float *gw = reinterpret_cast<float *>(scratch + L.gw);
   const StreamPlan pl = stream_plan(a.S, M, a.R, a.C, a.grad_Y != nullptr);
-  if (pl.ok && pl.grid <= 256 &&
+  if (pl.ok && pl.grid <= 512 &&
       !((reinterpret_cast<uintptr_t>(a.Hd) | reinterpret_cast<uintptr_t>(ms ? a.Hr : a.Hd)) & 15)) {
     float *Pp = reinterpret_cast<float *>(scratch + L.Pp);
     double *lp = reinterpret_cast<double *>(scratch + L.lp);
-    float *GUs = reinterpret_cast<float *>(scratch + L.GUs);
     unsigned *err = reinterpret_cast<unsigned *>(scratch + L.inv + 48);
-    if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Um, Pp, lp, GUs, gw, counter + 1, err, st);
-    return run_stream<2>(a, pl, M, Um, Pp, lp, GUs, gw, counter + 1, err, st);
+    if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Pp, lp, gw, counter + 1, err, st);
+    return run_stream<2>(a, pl, M, Pp, lp, gw, counter + 1, err, st);
   }
   switch (cbucket(a.C)) {
 #define CASE(CB) case CB: return run_cb<CB>(a, sp, M, Um, Ypart, G1, G2, part, counter, scal, GUp, gw, st);
