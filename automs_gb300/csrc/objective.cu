@@ -704,129 +704,125 @@ __global__ void __launch_bounds__(256, 2)
   }
 }
 
-// final of the streaming path.  Each CTA owns 32 metasurface rows: it reduces
-// their CTA partials G_U = sum P1 + (sum P2) / ||masked||, writes
-// dphi = -sum_c Im(conj(G_U) U) and partial sums of dL/dW; the last CTA adds
-// those and the H_d rows into grad_W.  Block 0 writes the loss.
+// final of the streaming path: one warp per row k of [H_r; H_d].
+// The warp reduces the row's CTA partials, G_U = sum P1 + (sum P2)/||masked||.
+// Metasurface rows write dphi = -sum_c Im(conj(G_U) U) (U recomputed) and add
+// G_U e^{-j phi'} conj(H_a[:, k]) to the CTA's dL/dW partial; H_d rows add
+// G_U itself.  The last CTA sums the CTA partials into grad_W, one warp per
+// entry.  Block 0 writes the loss.
 template <int CB>
 __global__ void __launch_bounds__(256) k_stream_final(ObjArgs a, int M, int nparts,
                                                       const float *Ppart, const double *lpart,
                                                       float *gw_part, unsigned *counter) {
-  __shared__ c2 gu[CB][32];
-  __shared__ c2 ph[32];
+  extern __shared__ float2 gw_s[];  // [C * S] partial dL/dW of this CTA
   __shared__ float inv_s;
   __shared__ bool last;
-  const int t = threadIdx.x, lane = t & 31;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int K = M + a.S;
-  const int m0 = blockIdx.x * 32;
-  const int nm = max(0, min(32, M - m0));
+  const int k = blockIdx.x * 8 + warp;
+  const int CS = a.C * a.S;
   const float2 *P = reinterpret_cast<const float2 *>(Ppart);
-  if (t < 32) {
+  for (int i = t; i < CS; i += blockDim.x) gw_s[i] = make_float2(0.f, 0.f);
+  if (warp == 0) {
     double x = 0, z = 0;
-    for (int b = t; b < nparts; b += 32) { x += lpart[2 * b]; z += lpart[2 * b + 1]; }
+    for (int b = lane; b < nparts; b += 32) { x += lpart[2 * b]; z += lpart[2 * b + 1]; }
     for (int o = 16; o > 0; o >>= 1) {
       x += __shfl_xor_sync(0xffffffffu, x, o);
       z += __shfl_xor_sync(0xffffffffu, z, o);
     }
-    if (t == 0) {
+    if (lane == 0) {
       const double nrm = sqrt(z);
       inv_s = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
       if (blockIdx.x == 0 && a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
     }
-    c2 e = {0.f, 0.f};
-    if (t < nm) {
-      const float pp = py_mod(__ldg(a.phi + m0 + t), a.max_phase);
-      sincosf(pp, &e.y, &e.x);
-    }
-    ph[t] = e;
   }
   __syncthreads();
   const float inv = inv_s;
-  // 8 threads per (c, row): each sums every 8th CTA partial
-  for (int e0 = 0; e0 < CB * 32; e0 += 32) {
-    const int e = e0 + (t >> 3), sub = t & 7;
-    const int c = e / 32, jj = e % 32;
-    c2 s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
-    if (c < a.C && jj < nm) {
+  if (k < K) {
+    c2 gu[CB];
+#pragma unroll
+    for (int c = 0; c < CB; c++) {
+      c2 s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
+      if (c < a.C) {
 #pragma unroll 4
-      for (int b = sub; b < nparts; b += 8) {
-        const float2 u = __ldcg(P + ((size_t)b * 2 * a.C + c) * K + m0 + jj);
-        s1.x += u.x; s1.y += u.y;
-        if (CB > 1) {
-          const float2 v = __ldcg(P + ((size_t)b * 2 * a.C + a.C + c) * K + m0 + jj);
-          s2.x += v.x; s2.y += v.y;
+        for (int b = lane; b < nparts; b += 32) {
+          const float2 u = __ldcg(P + ((size_t)b * 2 * a.C + c) * K + k);
+          s1.x += u.x; s1.y += u.y;
+          if (CB > 1) {
+            const float2 v = __ldcg(P + ((size_t)b * 2 * a.C + a.C + c) * K + k);
+            s2.x += v.x; s2.y += v.y;
+          }
         }
       }
-    }
-    for (int o = 1; o < 8; o <<= 1) {
-      s1.x += __shfl_xor_sync(0xffffffffu, s1.x, o);
-      s1.y += __shfl_xor_sync(0xffffffffu, s1.y, o);
-      s2.x += __shfl_xor_sync(0xffffffffu, s2.x, o);
-      s2.y += __shfl_xor_sync(0xffffffffu, s2.y, o);
-    }
-    if (sub == 0 && c < CB) gu[c][jj] = c2{fmaf(s2.x, inv, s1.x), fmaf(s2.y, inv, s1.y)};
-  }
-  __syncthreads();
-  if (a.grad_phi) {
-    // dphi[m] = -sum_c Im(conj(G_U) U) with U = (W H_a) e^{j phi'} recomputed,
-    // 8 lanes per row splitting the sum over the AP elements
-    const int jj = t >> 3, sub = t & 7;
-    float sacc = 0.f;
-    for (int c = 0; c < a.C; c++) {
-      c2 acc = {0.f, 0.f};
-      if (jj < nm)
-        for (int s2 = sub; s2 < a.S; s2 += 8)
-          mac(acc, ld2(a.W, (size_t)c * a.S + s2), ld2(a.Ha, (size_t)s2 * M + m0 + jj));
-      for (int o = 1; o < 8; o <<= 1) {
-        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+      for (int o = 16; o > 0; o >>= 1) {
+        s1.x += __shfl_xor_sync(0xffffffffu, s1.x, o);
+        s1.y += __shfl_xor_sync(0xffffffffu, s1.y, o);
+        s2.x += __shfl_xor_sync(0xffffffffu, s2.x, o);
+        s2.y += __shfl_xor_sync(0xffffffffu, s2.y, o);
       }
-      if (jj < nm) {
+      gu[c] = c2{fmaf(s2.x, inv, s1.x), fmaf(s2.y, inv, s1.y)};
+    }
+    if (k < M) {
+      c2 e;
+      const float pp = py_mod(__ldg(a.phi + k), a.max_phase);
+      sincosf(pp, &e.y, &e.x);
+      float sacc = 0.f;
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        if (c >= a.C) continue;
+        // U[c,k] = (sum_s W[c,s] H_a[s,k]) e^{j phi'}, lanes over s
+        c2 acc = {0.f, 0.f};
+        for (int s2 = lane; s2 < a.S; s2 += 32)
+          mac(acc, ld2(a.W, (size_t)c * a.S + s2), ld2(a.Ha, (size_t)s2 * M + k));
+        for (int o = 16; o > 0; o >>= 1) {
+          acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+          acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        }
         c2 u = {0.f, 0.f};
-        mac(u, acc, ph[jj]);
-        const c2 g = gu[c][jj];
-        sacc += g.x * u.y - g.y * u.x;  // Im(conj(g) u)
+        mac(u, acc, e);
+        sacc += gu[c].x * u.y - gu[c].y * u.x;  // Im(conj(g) u)
+        const c2 gv = {gu[c].x * e.x + gu[c].y * e.y, gu[c].y * e.x - gu[c].x * e.y};
+        if (a.grad_W)
+          for (int s2 = lane; s2 < a.S; s2 += 32) {
+            c2 d = {0.f, 0.f};
+            macc(d, gv, ld2(a.Ha, (size_t)s2 * M + k));
+            atomicAdd(&gw_s[c * a.S + s2].x, d.x);
+            atomicAdd(&gw_s[c * a.S + s2].y, d.y);
+          }
+      }
+      if (lane == 0 && a.grad_phi) a.grad_phi[k] = -sacc;
+    } else if (a.grad_W && lane == 0) {
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        if (c >= a.C) continue;
+        atomicAdd(&gw_s[c * a.S + (k - M)].x, gu[c].x);
+        atomicAdd(&gw_s[c * a.S + (k - M)].y, gu[c].y);
       }
     }
-    if (sub == 0 && jj < nm) a.grad_phi[m0 + jj] = -sacc;
   }
   if (!a.grad_W) return;
-  for (int i = t; i < a.C * a.S; i += blockDim.x) {
-    const int c = i / a.S, s2 = i % a.S;
-    c2 acc = {0.f, 0.f};
-    for (int jj = 0; jj < nm; jj++) {
-      const c2 g = gu[c][jj], e = ph[jj];
-      const c2 gv = {g.x * e.x + g.y * e.y, g.y * e.x - g.x * e.y};  // g e^{-j p}
-      macc(acc, gv, ld2(a.Ha, (size_t)s2 * M + m0 + jj));
-    }
-    reinterpret_cast<float2 *>(gw_part)[(size_t)blockIdx.x * a.C * a.S + i] = make_float2(acc.x, acc.y);
-  }
+  __syncthreads();
+  for (int i = t; i < CS; i += blockDim.x)
+    reinterpret_cast<float2 *>(gw_part)[(size_t)blockIdx.x * CS + i] = gw_s[i];
   __threadfence();
   __syncthreads();
   if (t == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
   __syncthreads();
   if (!last) return;
   __threadfence();
-  for (int i = t; i < a.C * a.S; i += blockDim.x) {
-    const int c = i / a.S, s2 = i % a.S;
-    c2 acc = {0.f, 0.f}, a2 = {0.f, 0.f};
-    for (int b = 0; b < nparts; b++) {
-      const float2 u = __ldcg(P + ((size_t)b * 2 * a.C + c) * K + M + s2);
-      acc.x += u.x; acc.y += u.y;
-      if (CB > 1) {
-        const float2 v = __ldcg(P + ((size_t)b * 2 * a.C + a.C + c) * K + M + s2);
-        a2.x += v.x; a2.y += v.y;
-      }
-    }
-    acc.x = fmaf(a2.x, inv, acc.x);
-    acc.y = fmaf(a2.y, inv, acc.y);
-    const float2 *gp = reinterpret_cast<const float2 *>(gw_part);
+  const float2 *gp = reinterpret_cast<const float2 *>(gw_part);
+  for (int i = warp; i < CS; i += 8) {
+    c2 acc = {0.f, 0.f};
 #pragma unroll 4
-    for (int b = 0; b < (int)gridDim.x; b++) {
-      const float2 u = __ldcg(gp + (size_t)b * a.C * a.S + i);
+    for (int b = lane; b < (int)gridDim.x; b += 32) {
+      const float2 u = __ldcg(gp + (size_t)b * CS + i);
       acc.x += u.x; acc.y += u.y;
     }
-    reinterpret_cast<float2 *>(a.grad_W)[i] = make_float2(acc.x, acc.y);
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane == 0) reinterpret_cast<float2 *>(a.grad_W)[i] = make_float2(acc.x, acc.y);
   }
   if (t == 0) *counter = 0u;  // ready for the next call
 }
@@ -956,8 +952,9 @@ cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *Ppa
     default: e = launch_stream_k<CB, 2>(a, pl, mr, md, M, Ppart, lpart, err, st); break;
   }
   if (e != cudaSuccess) return e;
-  const int nbf = std::max(1, (M + 31) / 32);
-  k_stream_final<CB><<<nbf, 256, 0, st>>>(a, M, pl.grid, Ppart, lpart, gw_part, counter);
+  const int nbf = (M + a.S + 7) / 8;
+  k_stream_final<CB><<<nbf, 256, sizeof(float2) * a.C * a.S, st>>>(a, M, pl.grid, Ppart, lpart,
+                                                                     gw_part, counter);
   return cudaGetLastError();
 }
 
@@ -970,7 +967,7 @@ ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
   size_t o = 0;
   L.inv = o; o += 256;                                    // control block (see header)
   L.Um = o; o += al(8 * (size_t)C * std::max(M, 1));      // U = (W H_a) e^{j phi'}
-  L.gw = o; o += al(8 * (size_t)std::max(1, (M + 31) / 32) * C * S);  // dL/dW partials
+  L.gw = o; o += al(8 * (size_t)std::max((M + 31) / 32, (M + S + 7) / 8) * C * S);  // dL/dW partials
   L.U = o; o += al(8 * (size_t)sp.kspl * C * R);          // Y partials
   L.G1 = o; o += al(8 * (size_t)C * R);
   L.G2 = o; o += al(8 * (size_t)C * R);
