@@ -69,6 +69,33 @@ __device__ __forceinline__ const float *row_ptr(const float *Hr, const float *Hd
 
 constexpr int KCHUNK = 256;
 
+// U[c, m] for the streaming path: 8 lanes per (m, c) split the sum over the
+// AP elements; the dependent streaming kernel may start before this one ends
+// (programmatic dependent launch) and waits for it only before reading U.
+__global__ void __launch_bounds__(256) k_prep_wide(ObjArgs a, int M, float *U) {
+  // let the streaming kernel launch now; it waits for this grid before reading U
+  cudaTriggerProgrammaticLaunchCompletion();
+  const long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+  const int sub = threadIdx.x & 7;
+  const bool live = e < (long long)M * a.C;
+  const int c = live ? (int)(e / M) : 0, m = live ? (int)(e % M) : 0;
+  c2 v = {0.f, 0.f};
+  if (live)
+    for (int s = sub; s < a.S; s += 8) mac(v, ld2(a.W, (size_t)c * a.S + s), ld2(a.Ha, (size_t)s * M + m));
+  for (int o = 1; o < 8; o <<= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  if (live && sub == 0) {
+    const float p = py_mod(__ldg(a.phi + m), a.max_phase);
+    float sn, cs;
+    sincosf(p, &sn, &cs);
+    c2 u = {0.f, 0.f};
+    mac(u, v, c2{cs, sn});
+    reinterpret_cast<float2 *>(U)[(size_t)c * M + m] = make_float2(u.x, u.y);
+  }
+}
+
 // U[c, m] = (sum_s W[c, s] H_a[s, m]) e^{j phi'_m}: one thread per (m, c),
 // loads of H_a coalesced over m, issued 8 at a time
 __global__ void __launch_bounds__(128) k_prep(ObjArgs a, int M, float *U) {
@@ -490,7 +517,8 @@ template <int CB, int TR, int KPT>
 __global__ void __launch_bounds__(256, 2)
     k_obj_stream(ObjArgs a, const __grid_constant__ CUtensorMap mapR,
                  const __grid_constant__ CUtensorMap mapD, int M, int Mbox, int Mp, int boxR,
-                 int stage_bytes, int ntiles, float *Ppart, double *lpart, unsigned *err) {
+                 int stage_bytes, int ntiles, const float *U, float *Ppart, double *lpart,
+                 unsigned *err) {
   constexpr int NTH = 256, NW = NTH / 32;
   const int K = M + a.S;
   // H_r rows [0, Mbox) come from boxes of boxR rows, H_d rows start at Mp
@@ -534,34 +562,13 @@ __global__ void __launch_bounds__(256, 2)
     if (first < ntiles) issue(first, 0);
     if (first + (int)gridDim.x < ntiles) issue(first + gridDim.x, 1);
   }
-  // coefficients while the first tiles are in flight: U = (W H_a) e^{j phi'}
-  // for metasurface rows, W for the H_d rows
+  // the first tiles are in flight; wait for the U kernel, then stage the
+  // coefficients: U for metasurface rows, W for the H_d rows
+  cudaGridDependencySynchronize();
   for (int i = t; i < K * CB; i += NTH) {
     const int k = i / CB, c = i % CB;
     c2 v = {0.f, 0.f};
-    if (c < a.C) {
-      if (k < M) {
-        c2 acc = {0.f, 0.f};
-        int s2 = 0;
-        for (; s2 + 8 <= a.S; s2 += 8) {
-          c2 h[8], w[8];
-#pragma unroll
-          for (int q = 0; q < 8; q++) {
-            h[q] = ld2(a.Ha, (size_t)(s2 + q) * M + k);
-            w[q] = ld2(a.W, (size_t)c * a.S + s2 + q);
-          }
-#pragma unroll
-          for (int q = 0; q < 8; q++) mac(acc, w[q], h[q]);
-        }
-        for (; s2 < a.S; s2++) mac(acc, ld2(a.W, (size_t)c * a.S + s2), ld2(a.Ha, (size_t)s2 * M + k));
-        const float pp = py_mod(__ldg(a.phi + k), a.max_phase);
-        float sn, cs;
-        sincosf(pp, &sn, &cs);
-        mac(v, acc, c2{cs, sn});
-      } else {
-        v = ld2(a.W, (size_t)c * a.S + (k - M));
-      }
-    }
+    if (c < a.C) v = k < M ? ld2(U, (size_t)c * M + k) : ld2(a.W, (size_t)c * a.S + (k - M));
     coef[i] = v;
   }
   __syncthreads();
@@ -907,8 +914,8 @@ StreamPlan stream_plan(int S, int M, int R, int C, bool grad_y) {
 
 template <int CB, int TR, int KPT>
 cudaError_t launch_stream_t(const ObjArgs &a, const StreamPlan &pl, const CUtensorMap &mr,
-                            const CUtensorMap &md, int M, float *Ppart, double *lpart,
-                            unsigned *err, cudaStream_t st) {
+                            const CUtensorMap &md, int M, const float *U, float *Ppart,
+                            double *lpart, unsigned *err, cudaStream_t st) {
   auto kfn = k_obj_stream<CB, TR, KPT>;
   static size_t set_bytes = 0;
   if (set_bytes < pl.smem) {
@@ -917,27 +924,36 @@ cudaError_t launch_stream_t(const ObjArgs &a, const StreamPlan &pl, const CUtens
     if (e != cudaSuccess) return e;
     set_bytes = pl.smem;
   }
-  kfn<<<pl.grid, 256, pl.smem, st>>>(a, mr, md, M, pl.Mbox, pl.Mp, pl.boxR, pl.stage_bytes,
-                                      pl.ntiles, Ppart, lpart, err);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(pl.grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = pl.smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kfn, a, mr, md, M, pl.Mbox, pl.Mp, pl.boxR, pl.stage_bytes,
+                            pl.ntiles, U, Ppart, lpart, err);
 }
 
 template <int CB, int TR>
 cudaError_t launch_stream_k(const ObjArgs &a, const StreamPlan &pl, const CUtensorMap &mr,
-                            const CUtensorMap &md, int M, float *Ppart, double *lpart,
-                            unsigned *err, cudaStream_t st) {
+                            const CUtensorMap &md, int M, const float *U, float *Ppart,
+                            double *lpart, unsigned *err, cudaStream_t st) {
   switch (pl.KPT) {
-    case 4: return launch_stream_t<CB, TR, 4>(a, pl, mr, md, M, Ppart, lpart, err, st);
-    case 8: return launch_stream_t<CB, TR, 8>(a, pl, mr, md, M, Ppart, lpart, err, st);
+    case 4: return launch_stream_t<CB, TR, 4>(a, pl, mr, md, M, U, Ppart, lpart, err, st);
+    case 8: return launch_stream_t<CB, TR, 8>(a, pl, mr, md, M, U, Ppart, lpart, err, st);
     case 16:
-      if (CB == 1) return launch_stream_t<1, TR, 16>(a, pl, mr, md, M, Ppart, lpart, err, st);
+      if (CB == 1) return launch_stream_t<1, TR, 16>(a, pl, mr, md, M, U, Ppart, lpart, err, st);
       return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
   }
 }
 
 template <int CB>
-cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *Ppart,
+cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, float *Ppart,
                        double *lpart, float *gw_part, unsigned *counter, unsigned *err,
                        cudaStream_t st) {
   CUtensorMap mr, md;
@@ -945,11 +961,15 @@ cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *Ppa
   if (!make_cmap(&mr, Hr, std::max(M, 1), a.R, pl.TR, pl.boxR) ||
       !make_cmap(&md, a.Hd, a.S, a.R, pl.TR, a.S))
     return cudaErrorInvalidValue;
+  if (M > 0) {
+    const long long n = (long long)M * a.C * 8;
+    k_prep_wide<<<(int)((n + 255) / 256), 256, 0, st>>>(a, M, U);
+  }
   cudaError_t e;
   switch (pl.TR) {
-    case 8: e = launch_stream_k<CB, 8>(a, pl, mr, md, M, Ppart, lpart, err, st); break;
-    case 4: e = launch_stream_k<CB, 4>(a, pl, mr, md, M, Ppart, lpart, err, st); break;
-    default: e = launch_stream_k<CB, 2>(a, pl, mr, md, M, Ppart, lpart, err, st); break;
+    case 8: e = launch_stream_k<CB, 8>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
+    case 4: e = launch_stream_k<CB, 4>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
+    default: e = launch_stream_k<CB, 2>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
   }
   if (e != cudaSuccess) return e;
   const int nbf = (M + a.S + 7) / 8;
@@ -1003,8 +1023,8 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
     float *Pp = reinterpret_cast<float *>(scratch + L.Pp);
     double *lp = reinterpret_cast<double *>(scratch + L.lp);
     unsigned *err = reinterpret_cast<unsigned *>(scratch + L.inv + 48);
-    if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Pp, lp, gw, counter + 1, err, st);
-    return run_stream<2>(a, pl, M, Pp, lp, gw, counter + 1, err, st);
+    if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Um, Pp, lp, gw, counter + 1, err, st);
+    return run_stream<2>(a, pl, M, Um, Pp, lp, gw, counter + 1, err, st);
   }
   switch (cbucket(a.C)) {
 #define CASE(CB) case CB: return run_cb<CB>(a, sp, M, Um, Ypart, G1, G2, part, counter, scal, GUp, gw, st);
