@@ -306,81 +306,6 @@ __device__ void traverse(const BvhNode *nodes, const float4 *prims, int n, const
 
 // optixTrace with a visibility mask: bit i selects instance i (0 scene,
 // 1 Tx spheres, 2 Rx spheres), optixPathTracer.cpp:417-424
-// ---------------------------------------------------- line-candidate cache
-// Within one branch slot the ray direction is fixed and the origin only moves
-// forward along the same line (Rx-sphere hits restart from the closest
-// approach point).  After the first Rx hit, every primitive whose widened box
-// meets the line before the next scene hit (plus slack) is gathered once,
-// sorted by box entry; later closest-hit queries from points further along
-// the line run the exact primitive tests over that list only.  Every
-// primitive that can be hit from those points is in the list (its hit point
-// lies in its box), so the answer equals a full traversal.
-#define AMS_CAND 128
-
-struct Cand { float tin, tout; int ref; };  // ref = sorted index | instance << 30
-
-__device__ __forceinline__ bool cand_push(Cand *c, int &nc, float tin, float tout, int ref) {
-  if (nc >= AMS_CAND) return false;
-  int i = nc++;
-  while (i > 0 && c[i - 1].tin > tin) { c[i] = c[i - 1]; i--; }
-  c[i].tin = tin; c[i].tout = tout; c[i].ref = ref;
-  return true;
-}
-
-// conservative box test over [0, tlim] that also reports the exit parameter
-__device__ __forceinline__ bool gather_test(const RayT &r, float lx, float ly, float lz, float hx,
-                                            float hy, float hz, float tlim, float &tn_out,
-                                            float &tf_out) {
-  float tx0 = __fmaf_rn(lx, r.inv.x, -r.oix), tx1 = __fmaf_rn(hx, r.inv.x, -r.oix);
-  float ty0 = __fmaf_rn(ly, r.inv.y, -r.oiy), ty1 = __fmaf_rn(hy, r.inv.y, -r.oiy);
-  float tz0 = __fmaf_rn(lz, r.inv.z, -r.oiz), tz1 = __fmaf_rn(hz, r.inv.z, -r.oiz);
-  float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-  float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-  tn_out = tn;
-  tf_out = tf;
-  return tn <= __fmaf_rn(tf, 1.0001f, 1e-5f) && tf >= -1e-5f && tn <= __fmaf_rn(tlim, 1.0001f, 1e-4f);
-}
-
-// collect the leaves whose boxes meet the ray within [0, tlim]; false on overflow
-template <int INST>
-__device__ bool gather(const BvhNode *nodes, int n, const RayT &r, float tlim, Cand *cand,
-                       int &nc, unsigned *err) {
-  if (n <= 0) return true;
-  if (n == 1) return cand_push(cand, nc, 0.0f, AMS_TMAX, 0 | (INST << 30));
-  int st_node[AMS_STACK];
-  int sp = 0, node = 0;
-  while (true) {
-    if ((unsigned)node >= (unsigned)(n - 1)) { atomicOr(err, AMS_DERR_BVH); return false; }
-    const float4 *np = reinterpret_cast<const float4 *>(nodes + node);
-    const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
-    const int4 d = __ldg(reinterpret_cast<const int4 *>(np + 3));
-    float tn0, tf0, tn1, tf1;
-    bool h0 = gather_test(r, a.x, a.y, a.z, a.w, b.x, b.y, tlim, tn0, tf0);
-    bool h1 = gather_test(r, b.z, b.w, c.x, c.y, c.z, c.w, tlim, tn1, tf1);
-    if (h0 && d.x < 0) {
-      if (~d.x >= n || !cand_push(cand, nc, tn0, tf0, (~d.x) | (INST << 30))) return false;
-      h0 = false;
-    }
-    if (h1 && d.y < 0) {
-      if (~d.y >= n || !cand_push(cand, nc, tn1, tf1, (~d.y) | (INST << 30))) return false;
-      h1 = false;
-    }
-    if (h0 && h1) {
-      if (sp >= AMS_STACK) { atomicOr(err, AMS_DERR_STACK); return false; }
-      st_node[sp++] = d.y;
-      node = d.x;
-    } else if (h0) {
-      node = d.x;
-    } else if (h1) {
-      node = d.y;
-    } else {
-      if (sp == 0) break;
-      node = st_node[--sp];
-    }
-  }
-  return true;
-}
-
 __device__ __forceinline__ Hit closest(const TraceDev &P, af3 o, af3 d, int mask) {
   RayT r;
   ray_setup(r, o, d);
@@ -477,28 +402,6 @@ __device__ int path_insert(const TraceDev &P, const int32_t *key) {
 }
 
 // scene triangle by original primitive index (optixPathTracer.cu:296-299)
-// closest hit among the cached candidates, from a point tau further along
-// the gathering ray; `start` skips candidates left behind
-__device__ __forceinline__ Hit closest_cand(const TraceDev &P, af3 o, af3 d, const Cand *cand,
-                                            int nc, int &start, float tau) {
-  RayT r;
-  ray_setup(r, o, d);
-  Hit h;
-  h.t = AMS_TMAX; h.inst = 3; h.prim = 0x7fffffff;
-  for (int i = start; i < nc; i++) {
-    const Cand c = cand[i];
-    if (c.tin - tau > __fmaf_rn(h.t, 1.0001f, 1e-4f)) break;
-    if (c.tout - tau < -1e-4f) {
-      if (i == start) start++;
-      continue;
-    }
-    const int j = c.ref & 0x3fffffff;
-    if ((c.ref >> 30) == 0) test_prim<0>(P.tri_prims, j, r, h, 0.0f);
-    else test_prim<2>(P.rx_prims, j, r, h, P.dst_r);
-  }
-  return h;
-}
-
 __device__ __forceinline__ void scene_tri(const TraceDev &P, int prim, af3 &v0, af3 &v1, af3 &v2) {
   const float *v = P.tris + (size_t)prim * 9;
   v0 = mk3(__ldg(v), __ldg(v + 1), __ldg(v + 2));
@@ -526,7 +429,6 @@ __global__ void __launch_bounds__(128) k_stage1(TraceDev P) {
     int res_cnt = 0;
     int rec[AMS_MAX_RESERVE];  // cell * 8 + hit_cnt of the records kept so far
     Slot slots[32];
-    Cand cand[AMS_CAND];
     const int L = P.L;
     for (int launch = 0; launch < P.spl; launch++) {
       float rs = rnd(seed) * (float)P.n_src;
@@ -545,35 +447,12 @@ __global__ void __launch_bounds__(128) k_stage1(TraceDev P) {
         af3 o = slots[i].o, d = slots[i].d;
         int ttl = slots[i].ttl;
         int guard = 0;
-        bool cached = false, no_cache = false;
-        int nc = 0, cstart = 0;
-        float tau = 0.0f;
         while (ttl > 0) {
           if (++guard > AMS_SEG_CAP) { atomicOr(P.err, AMS_DERR_LOOP); break; }
-          Hit h = cached ? closest_cand(P, o, d, cand, nc, cstart, tau) : closest(P, o, d, 5);
+          Hit h = closest(P, o, d, 5);
           my_segs++;
           if (h.inst == 3) break;
           o = add3(o, scl3(d, h.t));
-          if (h.inst == 2) {
-            if (cached) {
-              tau += h.t;
-            } else if (!no_cache) {
-              // gather the line's candidates up to the next scene hit
-              RayT r;
-              ray_setup(r, o, d);
-              Hit hs;
-              hs.t = AMS_TMAX; hs.inst = 3; hs.prim = 0x7fffffff;
-              traverse<0>(P.tri_nodes, P.tri_prims, P.n_tri, r, hs, 0.0f, P.err);
-              nc = 0;
-              cstart = 0;
-              tau = 0.0f;
-              cached = gather<0>(P.tri_nodes, P.n_tri, r, hs.t, cand, nc, P.err) &&
-                       gather<2>(P.rx_nodes, P.n_dst, r, hs.t, cand, nc, P.err);
-              no_cache = !cached;
-            }
-          } else {
-            cached = false;  // the origin moved past the gathered stretch
-          }
           if (h.inst == 0 && ttl > 1) {
             af3 v0, v1, v2;
             scene_tri(P, h.prim, v0, v1, v2);
