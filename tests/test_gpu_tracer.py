@@ -108,6 +108,21 @@ def test_full_coverage_config_properties(tracer):
     assert float(db.max()) < 0.0  # no gain above free space at these distances
 
 
+def test_full_coverage_parity_with_oracle(tracer):
+    """The full 128x128 Rx grid with 1M rays, L=2: stats, path list and ray
+    set identical to the oracle's (about 10 s of oracle time on 16 cores)."""
+    from automs_gb300 import scenes
+    c = scenes.coverage_config("coverage-128")
+    H, st, paths = run_gpu(tracer, c)
+    Ho, so, po = oracle.trace_channel(c["tris"], c["mat"], c["mat_prop"], c["src"], c["dst"],
+                                      c["params"])
+    for k in cases.STAT_KEYS + ("tasks", "overflow"):
+        assert st[k] == so[k], (k, st[k], so[k])
+    assert np.array_equal(paths, po)
+    assert np.array_equal(H != 0, Ho != 0)
+    assert rel(H, Ho) < 1e-5
+
+
 def test_launch_pathtrace_dropin(tracer):
     c = cases.channel_case("tiny")
     p = c["params"]
