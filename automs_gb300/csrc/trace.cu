@@ -131,7 +131,8 @@ __device__ __forceinline__ float beampattern(af3 d1, af3 d2, int type) {
 
 // ------------------------------------------------------------ primitives
 struct RayT {
-  af3 o, d, inv;
+  af3 o, d;
+  af3 inv;              // 1 / d clamped to +-1e30 (exact wherever it is smaller)
   float oix, oiy, oiz;  // o * inv for the node test
   int kx, ky, kz;
   float Sx, Sy, Sz;
@@ -140,7 +141,15 @@ struct RayT {
 __device__ __forceinline__ void ray_setup(RayT &r, af3 o, af3 d) {
   r.o = o;
   r.d = d;
-  r.inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  // The fused node test computes lo * inv - o * inv.  For an axis-parallel
+  // ray (a zero direction component) an infinite inverse would give
+  // inf - inf = NaN, or -inf for a box that reaches below 0, and cull nodes
+  // the ray is inside of.  The clamp keeps every term finite; node boxes are
+  // widened far beyond its rounding error.  prim_slab recovers the exact
+  // inverse where the clamp applies.
+  const float big = 1e30f;
+  r.inv = mk3(fminf(fmaxf(1.0f / d.x, -big), big), fminf(fmaxf(1.0f / d.y, -big), big),
+              fminf(fmaxf(1.0f / d.z, -big), big));
   r.oix = o.x * r.inv.x;
   r.oiy = o.y * r.inv.y;
   r.oiz = o.z * r.inv.z;
@@ -183,10 +192,17 @@ __device__ __forceinline__ float tri_hit(const RayT &r, af3 v0, af3 v1, af3 v2) 
 }
 
 // slab gate in front of the sphere program (AABB given by the caller)
+// exact 1 / d from the clamped inverse (recomputed only where clamped)
+__device__ __forceinline__ float exact_inv(float clamped, float d) {
+  return fabsf(clamped) < 1e30f ? clamped : 1.0f / d;
+}
+
 __device__ __forceinline__ bool prim_slab(const RayT &r, float4 lo, float4 hi) {
-  float tx0 = (lo.x - r.o.x) * r.inv.x, tx1 = (hi.x - r.o.x) * r.inv.x;
-  float ty0 = (lo.y - r.o.y) * r.inv.y, ty1 = (hi.y - r.o.y) * r.inv.y;
-  float tz0 = (lo.z - r.o.z) * r.inv.z, tz1 = (hi.z - r.o.z) * r.inv.z;
+  const float ix = exact_inv(r.inv.x, r.d.x), iy = exact_inv(r.inv.y, r.d.y),
+              iz = exact_inv(r.inv.z, r.d.z);
+  float tx0 = (lo.x - r.o.x) * ix, tx1 = (hi.x - r.o.x) * ix;
+  float ty0 = (lo.y - r.o.y) * iy, ty1 = (hi.y - r.o.y) * iy;
+  float tz0 = (lo.z - r.o.z) * iz, tz1 = (hi.z - r.o.z) * iz;
   float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
   float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
   return tn <= tf && tf >= AMS_TMIN && tn <= AMS_TMAX;
@@ -418,7 +434,7 @@ struct Slot {
 
 
 
-__global__ void __launch_bounds__(128) k_stage1(TraceDev P) {
+__global__ void __launch_bounds__(128, 7) k_stage1(TraceDev P) {
   const long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long n_launch = (long long)P.launch_x * P.launch_y;
   unsigned long long my_records = 0, my_segs = 0;
@@ -551,7 +567,7 @@ __global__ void k_make_tasks(TraceDev P, const unsigned *bits) {
 }
 
 // ---------------------------------------------------------------- stage 2
-__global__ void __launch_bounds__(256) k_stage2(TraceDev P, unsigned long long n_tasks) {
+__global__ void __launch_bounds__(256, 4) k_stage2(TraceDev P, unsigned long long n_tasks) {
   const int S = P.n_src;
   const int per_cell = P.gs * P.gs;
   const unsigned long long per_task = (unsigned long long)per_cell * S;

@@ -34,18 +34,21 @@ def _quad_grid(p0, u, v, nu, nv):
 
 
 def box_tris(lo, hi, n=1):
+    """12 n^2 triangles of an axis-aligned box; n may be a pair (nu, nv) of
+    quads per face side."""
+    nu, nv = (n, n) if np.isscalar(n) else n
     lo = np.asarray(lo, np.float64)
     hi = np.asarray(hi, np.float64)
     ex = np.array([hi[0] - lo[0], 0, 0])
     ey = np.array([0, hi[1] - lo[1], 0])
     ez = np.array([0, 0, hi[2] - lo[2]])
     tris = []
-    tris += _quad_grid(lo, ex, ey, n, n)            # bottom
-    tris += _quad_grid(lo + ez, ex, ey, n, n)       # top
-    tris += _quad_grid(lo, ex, ez, n, n)            # y = lo
-    tris += _quad_grid(lo + ey, ex, ez, n, n)       # y = hi
-    tris += _quad_grid(lo, ey, ez, n, n)            # x = lo
-    tris += _quad_grid(lo + ex, ey, ez, n, n)       # x = hi
+    tris += _quad_grid(lo, ex, ey, nu, nv)            # bottom
+    tris += _quad_grid(lo + ez, ex, ey, nu, nv)       # top
+    tris += _quad_grid(lo, ex, ez, nu, nv)            # y = lo
+    tris += _quad_grid(lo + ey, ex, ez, nu, nv)       # y = hi
+    tris += _quad_grid(lo, ey, ez, nu, nv)            # x = lo
+    tris += _quad_grid(lo + ex, ey, ez, nu, nv)       # x = hi
     return tris
 
 
@@ -147,6 +150,82 @@ def coverage_config(name="coverage-128", seed=0):
                   dst_gridsize=5, src_r=0.5e-5, dst_r=0.06,
                   src_dir=[0.0, 1.0, 0.0], dst_dir=[0.0, 0.0, 0.0])
     return dict(tris=tris, mat=mat, mat_prop=mat_prop, src=src, dst=dst, params=params)
+
+
+def metasurface(center, normal, down, n, spacing, thickness=1e-3):
+    """Element positions [n, n, 3], blackhole quad [2, 3, 3] and unit normal of
+    an n x n metasurface (gen_ms, go.py:388-443), in numpy float32."""
+    k = np.asarray(normal, np.float64)
+    k = k / np.linalg.norm(k)
+    i = np.asarray(down, np.float64)
+    j = np.cross(k, i)
+    i = i / np.linalg.norm(i)
+    j = j / np.linalg.norm(j)
+    c = np.asarray(center, np.float64) + k * thickness
+    u = np.linspace(-(n - 1) / 2, (n - 1) / 2, n)
+    pos = c + (u[:, None, None] * i + u[None, :, None] * j) * spacing
+    io, jo = i * n / 2 * spacing, j * n / 2 * spacing
+    ul, dr, ur, dl = c - io - jo, c + io + jo, c + io - jo, c - io + jo
+    quad = np.array([[ul, ur, dl], [dl, dr, ur]], np.float32)
+    return pos.astype(np.float32), quad, k.astype(np.float32)
+
+
+def with_blackholes(tris, mat, mat_prop, quads):
+    """Append blackhole quads (an all-zero material row, go.py:708-716)."""
+    if len(quads) == 0:
+        return tris, mat, mat_prop
+    q = np.asarray(quads, np.float32).reshape(-1, 3, 3)
+    return (np.concatenate([tris, q], 0),
+            np.concatenate([mat, np.full(q.shape[0], mat_prop.shape[0], np.int32)]),
+            np.concatenate([mat_prop, np.zeros((1, 19), np.float32)], 0))
+
+
+def channel_ms_config(name="ms-256", seed=0):
+    """Channel set with one metasurface: AP->Rx (the metasurface a
+    blackhole), AP->MS and MS->Rx traces (build_channels, go.py:1135-1247).
+
+    ms-256: 12x8x3 m room with 200 boxes, 5x4 quads per box face and 13x13
+      per room face (50,028 triangles); 16-element ULA at (6, 0.5, 2.5)
+      facing +y; 32x32 metasurface at lambda/2 on the y=8 wall centred at
+      (6, 8, 2), normal -y; 256x256 Rx grid at z=1.5; 1000x1000 launch;
+      3 reflections.
+    ms-small: 12 boxes with 1 quad per face, 6x6 metasurface, 20x20 Rx,
+      128x128 launch, 3 reflections (sized for the oracle).
+    """
+    lam = WAVE_LEN_60GHZ
+    tx_pos = (6.0, 0.5, 2.5)
+    ms_c = (6.0, 8.0 - 1e-3, 2.0)
+    if name == "ms-256":
+        tris, mat, mat_prop = shoebox_scene(200, box_tess=(5, 4), room_tess=13, seed=seed,
+                                            keep_clear=[tx_pos, ms_c])
+        n_src, n_ms, n_rx, launch = 16, 32, 256, 1000
+    elif name == "ms-small":
+        tris, mat, mat_prop = shoebox_scene(12, box_tess=1, seed=seed, keep_clear=[tx_pos, ms_c])
+        n_src, n_ms, n_rx, launch = 4, 6, 20, 128
+    else:
+        raise ValueError(name)
+    L = 3
+    src = ula(tx_pos, (1, 0, 0), n_src, lam / 2)
+    dst = rx_grid(0.25, 11.75, n_rx, 0.25, 7.75, n_rx, 1.5)
+    pos, quad, k = metasurface(ms_c, (0, -1, 0), (0, 0, -1), n_ms, lam / 2)
+
+    def prm(sbp, dbp, sdir, ddir):
+        return dict(samples_per_launch=1, launch_x=launch, launch_y=launch, wave_len=lam,
+                    max_reflection=L, reserve_size=100, src_bptype=sbp, dst_bptype=dbp,
+                    dst_gridsize=5, src_r=0.5e-5, dst_r=0.06, src_dir=list(map(float, sdir)),
+                    dst_dir=list(map(float, ddir)))
+
+    ap_dir, none = (0.0, 1.0, 0.0), (0.0, 0.0, 0.0)
+    return dict(tris=tris, mat=mat, mat_prop=mat_prop, src=src, dst=dst, ms=pos,
+                blackhole=quad, normal=k,
+                traces={
+                    "src_to_dst": dict(src=src, dst=dst, blackhole=True,
+                                       params=prm(2, 0, ap_dir, none)),
+                    "src_to_ms{0}": dict(src=src, dst=pos, blackhole=False,
+                                         params=prm(2, 1, ap_dir, k)),
+                    "ms{0}_to_dst": dict(src=pos, dst=dst, blackhole=False,
+                                         params=prm(1, 0, k, none)),
+                })
 
 
 # ----------------------------------------------------------- STL scenes

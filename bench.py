@@ -209,6 +209,100 @@ def objective_bench(torch, steps, flush):
             "gpu_launches_per_eval": 4}
 
 
+def channel_ms_bench(torch, warmup, steps, flush):
+    """Channel set with one 32x32 metasurface on a 50k-triangle scene, 256x256
+    Rx grid, 3 reflections, 1000x1000 launches: the AP->Rx, AP->MS and MS->Rx
+    traces on resident scenes (Rx-paths/s over the three), then objective+grad
+    evaluations on the traced channels (S=16, M=1024, R=65536; H_r is 537 MB,
+    more than L2, so every evaluation streams it from HBM)."""
+    import ctypes as C
+
+    from automs_gb300 import scenes, tracer
+    from automs_gb300._lib import call
+    cfg = scenes.channel_ms_config("ms-256")
+    base = tracer.Scene(cfg["tris"], cfg["mat"], cfg["mat_prop"])
+    bh = tracer.Scene(*scenes.with_blackholes(cfg["tris"], cfg["mat"], cfg["mat_prop"],
+                                              [cfg["blackhole"]]))
+    jobs = []
+    for key, t in cfg["traces"].items():
+        sc = bh if t["blackhole"] else base
+        src = torch.as_tensor(t["src"], device="cuda")
+        dst = torch.as_tensor(t["dst"], device="cuda")
+        res = torch.zeros(src.shape[0] * src.shape[1], dst.shape[0] * dst.shape[1], 2,
+                          device="cuda")
+        jobs.append((key, sc, src, dst, tracer.params_from_dict(t["params"]), res))
+    stream = torch.cuda.current_stream()
+    per = {k: [] for k, *_ in jobs}
+    for it in range(warmup + steps):
+        for key, sc, src, dst, prm, res in jobs:
+            flush()
+            res.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _, st = sc.trace(src, dst, prm, result=res)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if it >= warmup:
+                per[key].append((e0.elapsed_time(e1), st))
+    base.close()
+    bh.close()
+    traces = {}
+    tot_ms, tot_paths = 0.0, 0
+    for key, v in per.items():
+        ms = sum(a for a, _ in v) / len(v)
+        st = v[0][1]
+        traces[key] = {"ms": ms, "rx_paths": st["rx_paths"], "tasks": st["tasks"],
+                       "unique_paths": st["unique_paths"], "rounds": st["rounds"],
+                       "ms_stage1": st["ms_stage1"], "ms_stage2": st["ms_stage2"],
+                       "segments_fwd": st["segments_fwd"], "segments_bwd": st["segments_bwd"]}
+        tot_ms += ms
+        tot_paths += st["rx_paths"]
+    # objective + adjoint on the traced channels, reference orientation
+    Hd, Ha, Hr = (r for _, _, _, _, _, r in jobs)
+    S, M, R = Ha.shape[0], Ha.shape[1], Hd.shape[1]
+    rng = np.random.Generator(np.random.PCG64(3))
+    phi = torch.as_tensor(rng.uniform(0, 2 * np.pi, M).astype(np.float32), device="cuda")
+    wv = rng.normal(size=S) + 1j * rng.normal(size=S)
+    W = torch.as_tensor((wv / np.linalg.norm(wv)).astype(np.complex64)[None], device="cuda")
+    loss = torch.empty(1, device="cuda")
+    gW = torch.empty(1, S, dtype=torch.complex64, device="cuda")
+    gphi = torch.empty(M, device="cuda")
+    P = lambda t: C.c_void_p(t.data_ptr())
+
+    def ev():
+        call("ams_objective_fwd_bwd", P(Hd), P(Ha), P(Hr), P(phi), float(2 * np.pi), P(W), S,
+             M, R, 1, 1.0 / R, C.c_void_p(0), P(loss), P(gW), P(gphi), C.c_void_p(0),
+             C.c_void_p(0), C.c_void_p(stream.cuda_stream))
+    for _ in range(5):
+        ev()
+    n_ev = 50
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(n_ev):
+        ev()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / n_ev
+    bytes_alg = 8 * (R * M + M * S + R * S)
+    hbm, kind = peaks()
+    achieved = bytes_alg / (t * 1e-3) / 1e9
+    return {"metric": "channel-set Rx-paths/s", "value": tot_paths / (tot_ms * 1e-3),
+            "unit": "Rx-paths/s", "ms_per_set": tot_ms, "steps": steps,
+            "config": {"workload": "ms-256: 50,028 triangles, 16-element ULA, 32x32 "
+                       "metasurface, 256x256 Rx, 1000x1000 launch, 3 reflections",
+                       "l2": "flushed before every trace (256 MB write)"},
+            "traces": traces,
+            "objective": {"metric": "objective+grad evals/s", "value": 1e3 / t,
+                          "ms_per_eval": t, "S": S, "M": M, "R": R, "C": 1,
+                          "l2": "H_r 537 MB > L2, back-to-back evaluations",
+                          "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
+                                       "unit": "GB/s", "frac": achieved / hbm,
+                                       "algorithmic_bytes": bytes_alg, "peak_kind": kind},
+                          "loss": float(loss)}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -216,7 +310,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "tracer", "objective"],
+    ap.add_argument("--only", default="all", choices=["all", "tracer", "objective", "ms"],
                     help="profiling aid: run only the named timed loop")
     ap.add_argument("--launch", type=int, default=0,
                     help="profiling aid: override the forward launch edge (default 1000)")
@@ -240,6 +334,11 @@ def main():
     cfg = scenes.coverage_config("coverage-128", seed=rank)
     if args.launch:
         cfg["params"]["launch_x"] = cfg["params"]["launch_y"] = args.launch
+    if args.only == "ms":
+        flushbuf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        print(json.dumps(channel_ms_bench(torch, 1, max(1, args.steps),
+                                          lambda: flushbuf.fill_(1.0))))
+        return
     if args.only == "objective":
         flushbuf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
         print(json.dumps(objective_bench(torch, args.steps, lambda: flushbuf.fill_(1.0))))

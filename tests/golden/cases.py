@@ -15,7 +15,10 @@ from automs_gb300 import scenes  # noqa: E402
 STAT_KEYS = ("rx_paths", "rx_fail", "fwd_records", "unique_records", "unique_paths", "rounds")
 
 CHANNEL_CASES = ("tiny", "small", "pen_l3", "allpen_l4", "ms_to_rx", "ap_to_ms",
-                 "bp3_door", "spl2_cap", "l0", "l5")
+                 "bp3_door", "spl2_cap", "l0", "l5", "ms3_ap_rx", "ms3_ap_ms", "ms3_ms_rx")
+
+# the three traces of the small one-metasurface channel set
+_MS3 = {"ms3_ap_rx": "src_to_dst", "ms3_ap_ms": "src_to_ms{0}", "ms3_ms_rx": "ms{0}_to_dst"}
 
 
 def _ms_array(n0, n1, center, normal, up, spacing):
@@ -32,6 +35,14 @@ def _ms_array(n0, n1, center, normal, up, spacing):
 
 def channel_case(name):
     lam = scenes.WAVE_LEN_60GHZ
+    if name in _MS3:
+        m = scenes.channel_ms_config("ms-small")
+        t = m["traces"][_MS3[name]]
+        tris, mat, mp = m["tris"], m["mat"], m["mat_prop"]
+        if t["blackhole"]:
+            tris, mat, mp = scenes.with_blackholes(tris, mat, mp, [m["blackhole"]])
+        return dict(tris=tris, mat=mat, mat_prop=mp, src=t["src"], dst=t["dst"],
+                    params=dict(t["params"]))
     if name in ("tiny", "pen_l3", "allpen_l4", "ms_to_rx", "bp3_door", "spl2_cap", "l0", "l5"):
         c = scenes.coverage_config("coverage-tiny")
     elif name in ("small", "ap_to_ms"):

@@ -42,8 +42,8 @@ def digest(*arrays):
     return h.hexdigest()
 
 
-def make_channel_fixtures():
-    for name in cases.CHANNEL_CASES:
+def make_channel_fixtures(names=cases.CHANNEL_CASES):
+    for name in names:
         c = cases.channel_case(name)
         H, st, paths = oracle.ref_trace_channel(c["tris"], c["mat"], c["mat_prop"],
                                                 c["src"], c["dst"], c["params"])
@@ -187,6 +187,9 @@ def make_objective_fixtures():
 if __name__ == "__main__":
     if not oracle.ref_available():
         raise SystemExit("reference tree not mounted; fixtures cannot be regenerated here")
+    if len(sys.argv) > 1:  # regenerate the named channel fixtures only
+        make_channel_fixtures(sys.argv[1:])
+        raise SystemExit(0)
     make_unit_fixtures()
     make_channel_fixtures()
     make_objective_fixtures()
