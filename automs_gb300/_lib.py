@@ -70,6 +70,11 @@ SIGNATURES = {
     "ams_objective_fwd_bwd_noalloc": (_I, [_P, _P, _P, _P, _F, _P, _I, _I, _I, _I, _F, _P, _P,
                                            _P, _P, _P, _P, _P, _E, _S]),
     "ams_objective_recv": (_I, [_P, _P, _P, _P, _F, _P, _I, _I, _I, _I, _P, _P, _E, _S]),
+    "ams_objective_plan_create": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, C.POINTER(_P), _E, _S]),
+    "ams_objective_plan_fwd_bwd": (_I, [_P, _P, _F, _P, _I, _F, _P, _P, _P, _P, _P, _P, _P, _E,
+                                        _S]),
+    "ams_objective_plan_bytes": (C.c_ulonglong, [_P]),
+    "ams_objective_plan_destroy": (None, [_P]),
     "ams_coverage_db": (_I, [_P, _I, _I, _F, _F, _P, _P, _E, _S]),
     "ams_scratch_bytes": (C.c_ulonglong, []),
     "ams_gemm_bf16": (_I, [_P, _P, _I, _I, _I, _P, _I, _P, _P, _P, _E, _S]),

@@ -575,6 +575,64 @@ ams_status ams_objective_fwd_bwd_noalloc(const float *H_d, const float *H_a, con
   return AMS_OK;
 }
 
+struct ams_objective_plan {
+  ObjTcPlan *p;
+  int S, M, R, Cmax;
+};
+
+ams_status ams_objective_plan_create(const float *H_d, const float *H_a, const float *H_r, int S,
+                                     int M, int R, int C_max, void *stream,
+                                     ams_objective_plan **out, char *errbuf, size_t errlen) {
+  if (!out) { set_err(errbuf, errlen, "out is NULL"); return AMS_ERR_ARG; }
+  *out = nullptr;
+  if (!H_d || !H_a || !H_r) {
+    set_err(errbuf, errlen, "a plan needs H_d, H_a and H_r");
+    return AMS_ERR_ARG;
+  }
+  if (S <= 0 || M <= 0 || R <= 0 || C_max <= 0 || C_max > 64) {
+    set_err(errbuf, errlen, "need S, M, R > 0 and 1 <= C_max <= 64 (S=%d M=%d R=%d C_max=%d)", S,
+            M, R, C_max);
+    return AMS_ERR_ARG;
+  }
+  if ((reinterpret_cast<uintptr_t>(H_d) | reinterpret_cast<uintptr_t>(H_a) |
+       reinterpret_cast<uintptr_t>(H_r)) & 7) {
+    set_err(errbuf, errlen, "complex arrays must be 8-byte aligned");
+    return AMS_ERR_ARG;
+  }
+  ObjTcPlan *tp = nullptr;
+  CK(obj_tc_plan_create(H_d, H_a, H_r, S, M, R, C_max, (cudaStream_t)stream, &tp));
+  *out = new ams_objective_plan{tp, S, M, R, C_max};
+  return AMS_OK;
+}
+
+ams_status ams_objective_plan_fwd_bwd(ams_objective_plan *plan, const float *phi, float max_phase,
+                                      const float *W, int C, float w, const uint8_t *drop,
+                                      float *loss, float *grad_W, float *grad_phi, float *grad_Y,
+                                      float *recv_amp, void *stream, char *errbuf,
+                                      size_t errlen) {
+  if (!plan || !plan->p) { set_err(errbuf, errlen, "plan is NULL"); return AMS_ERR_ARG; }
+  if (!phi || !W || !loss) { set_err(errbuf, errlen, "phi, W and loss are required"); return AMS_ERR_ARG; }
+  if (C <= 0 || C > plan->Cmax) {
+    set_err(errbuf, errlen, "C=%d outside [1, %d] of this plan", C, plan->Cmax);
+    return AMS_ERR_ARG;
+  }
+  if (!(max_phase > 0.f)) { set_err(errbuf, errlen, "max_phase must be > 0"); return AMS_ERR_ARG; }
+  ObjArgs a{nullptr, nullptr, nullptr, phi, W, max_phase, plan->S, plan->M, plan->R, C, w, drop,
+            loss, grad_W, grad_phi, recv_amp, grad_Y};
+  CK(obj_tc_run(plan->p, a, (cudaStream_t)stream));
+  return AMS_OK;
+}
+
+unsigned long long ams_objective_plan_bytes(const ams_objective_plan *plan) {
+  return plan ? (unsigned long long)obj_tc_plan_bytes(plan->p) : 0ull;
+}
+
+void ams_objective_plan_destroy(ams_objective_plan *plan) {
+  if (!plan) return;
+  obj_tc_plan_destroy(plan->p);
+  delete plan;
+}
+
 ams_status ams_objective_recv(const float *H_d, const float *H_a, const float *H_r,
                               const float *phi, float max_phase, const float *W, int S, int M,
                               int R, int C, float *recv_amp, void *stream, char *errbuf,

@@ -19,6 +19,7 @@
 // once.  Scratch lives in a per-device buffer kept across calls; calls on
 // one device must not overlap.
 #include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,6 +30,7 @@
 
 #include "../../include/ams.h"
 #include "objective.h"
+#include "tc_ptx.cuh"
 
 namespace {
 
@@ -978,6 +980,239 @@ cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, 
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------
+// Tensor-core path (tcgen05, 3xBF16 split precision, FP32 accumulation).
+//
+// A complex product over k becomes one real GEMM on interleaved real views;
+// output c occupies the accumulator rows 2c (real part) and 2c+1 (imaginary
+// part), which adjacent lanes of one warp read back.
+//   forward  Y[c, r] = sum_k coef[c, k] [H_r; H_d][k, r]       (pass 1)
+//     A_y row 2c = (Re coef, -Im coef) per k, row 2c+1 = (Im coef, Re coef)
+//     B_y = [H_r; H_d]^T as a real [R, 2K] matrix (row r: Re, Im of each k)
+//   adjoint  G_U[c, k] = sum_r G[c, r] conj([H_r; H_d][k, r])  (pass 2)
+//     A_g row 2c = (Re G, Im G) per r, row 2c+1 = (Im G, -Re G)
+//     B_g = [H_r; H_d] as a real [K, 2R] matrix (its native layout)
+// Each operand x is held as x_hi = bf16(x) and x_lo = bf16(x - x_hi); the
+// product is A_hi B_hi + A_hi B_lo + A_lo B_hi (the dropped A_lo B_lo term is
+// below 2^-16 of it).  B_y and B_g are built once per channel set (a plan);
+// an evaluation rebuilds only the small A operands.
+
+namespace tcg {
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3;
+constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
+constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+constexpr size_t SMEM = STAGES * STAGE_BYTES + 1024;
+}  // namespace tcg
+
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
+  hi = __float2bfloat16_rn(x);
+  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+__device__ __forceinline__ void put_pair(__nv_bfloat16 *hi, __nv_bfloat16 *lo, size_t pair,
+                                         float a, float b) {
+  __nv_bfloat16 h0, l0, h1, l1;
+  split_bf16(a, h0, l0);
+  split_bf16(b, h1, l1);
+  reinterpret_cast<__nv_bfloat162 *>(hi)[pair] = __halves2bfloat162(h0, h1);
+  reinterpret_cast<__nv_bfloat162 *>(lo)[pair] = __halves2bfloat162(l0, l1);
+}
+
+// B_y [Rp, Kp] from [H_r; H_d] [K, R] complex: 32 x 32 complex tiles turned
+// through shared memory (reads coalesced over r, writes over k); entries
+// beyond R or K are zero.  Block (32, 8), grid (Rp / 32, Kp / 64).
+__global__ void __launch_bounds__(256) k_tc_make_by(const float *Hr, const float *Hd, int M,
+                                                    int S, int R, int Rp, int Kp,
+                                                    __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+  __shared__ float2 t[32][33];
+  const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32, K = M + S;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int k = k0 + i, r = r0 + threadIdx.x;
+    float2 v = make_float2(0.f, 0.f);
+    if (k < K && r < R)
+      v = __ldg(reinterpret_cast<const float2 *>(k < M ? Hr + (size_t)k * R * 2
+                                                        : Hd + (size_t)(k - M) * R * 2) + r);
+    t[i][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = r0 + i, k = k0 + threadIdx.x;
+    if (r >= Rp || 2 * k >= Kp) continue;
+    const float2 v = t[threadIdx.x][i];
+    put_pair(hi, lo, ((size_t)r * Kp + 2 * k) / 2, v.x, v.y);
+  }
+}
+
+// B_g [Np, K2p] = [H_r; H_d] real view, zero padded; one thread per complex
+__global__ void k_tc_make_bg(const float *Hr, const float *Hd, int M, int S, int R, int Np,
+                             int K2p, __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long ncol = K2p / 2;
+  if (i >= (long long)Np * ncol) return;
+  const int k = (int)(i / ncol), r = (int)(i % ncol);
+  float2 v = make_float2(0.f, 0.f);
+  if (k < M + S && r < R)
+    v = __ldg(reinterpret_cast<const float2 *>(k < M ? Hr + (size_t)k * R * 2
+                                                      : Hd + (size_t)(k - M) * R * 2) + r);
+  put_pair(hi, lo, (size_t)i, v.x, v.y);
+}
+
+// A_y rows 2c, 2c+1 [., Kp] from coef[c, k] = U[c, k] (k < M), W[c, k - M]
+// (M <= k < M + S), zero beyond; one thread per (c, k), c < C
+__global__ void k_tc_make_ay(const float *U, const float *W, int C, int M, int S, int Kp,
+                             __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int kc = Kp / 2;
+  if (i >= (long long)C * kc) return;
+  const int c = (int)(i / kc), k = (int)(i % kc);
+  float2 v = make_float2(0.f, 0.f);
+  if (k < M) v = reinterpret_cast<const float2 *>(U)[(size_t)c * M + k];
+  else if (k < M + S) v = __ldg(reinterpret_cast<const float2 *>(W) + (size_t)c * S + (k - M));
+  put_pair(hi, lo, ((size_t)(2 * c) * Kp + 2 * k) / 2, v.x, -v.y);
+  put_pair(hi, lo, ((size_t)(2 * c + 1) * Kp + 2 * k) / 2, v.y, v.x);
+}
+
+// A_g rows 2c, 2c+1 [., K2p] from G = G1 + G2 / ||masked||; one thread per
+// (c, r), c < C
+__global__ void k_tc_make_ag(const float *G1, const float *G2, const float *scal, int C, int R,
+                             int K2p, __nv_bfloat16 *hi, __nv_bfloat16 *lo) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int rc = K2p / 2;
+  if (i >= (long long)C * rc) return;
+  const int c = (int)(i / rc), r = (int)(i % rc);
+  float2 g = make_float2(0.f, 0.f);
+  if (r < R) {
+    g = reinterpret_cast<const float2 *>(G1)[(size_t)c * R + r];
+    if (G2) {
+      const float inv = scal[0];
+      const float2 h = reinterpret_cast<const float2 *>(G2)[(size_t)c * R + r];
+      g.x = fmaf(h.x, inv, g.x);
+      g.y = fmaf(h.y, inv, g.y);
+    }
+  }
+  put_pair(hi, lo, ((size_t)(2 * c) * K2p + 2 * r) / 2, g.x, g.y);
+  put_pair(hi, lo, ((size_t)(2 * c + 1) * K2p + 2 * r) / 2, g.y, -g.x);
+}
+
+// D = sum over this CTA's k-blocks of A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T
+// for a 128 x 128 tile, A [Mp, Kd] and B [Np, Kd] bf16 with K contiguous.
+// Warp 0 / lane 0 feeds a 3-stage TMA ring (four 16 KB tiles per stage),
+// warp 1 / lane 0 issues 12 tcgen05.mma per stage, all 4 warps drain TMEM.
+// Rows 2c / 2c+1 of D are stored as out[(z * C + c) * ldo + n] (complex) for
+// c < C and n < n_valid, z = blockIdx.z (the split of the k range).
+__global__ void __launch_bounds__(128, 1)
+    k_cgemm3(const __grid_constant__ CUtensorMap tah, const __grid_constant__ CUtensorMap tal,
+             const __grid_constant__ CUtensorMap tbh, const __grid_constant__ CUtensorMap tbl,
+             int kb_per, int nkb, int C, int n_valid, long long ldo, float *out, unsigned *err) {
+  using namespace tcg;
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *smem = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
+  const int kb0 = blockIdx.z * kb_per;
+  const int nk = min(kb_per, nkb - kb0);  // >= 1: the host sizes the grid so
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; s++) { tc::mbar_init(&full[s], 1); tc::mbar_init(&empty[s], 1); }
+    tc::mbar_init(&done, 1);
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, (uint32_t)BN);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    for (int kb = 0; kb < nk; kb++) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES && !tc::mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1)) {
+        abort_flag = 1;
+        atomicOr(err, 1u);
+        break;
+      }
+      if (*(volatile int *)&abort_flag) break;
+      unsigned char *sp = smem + s * STAGE_BYTES;
+      const int x = (kb0 + kb) * BK;
+      tc::mbar_expect_tx(&full[s], STAGE_BYTES);
+      tc::tma_load_2d(sp, &tah, x, m0, &full[s]);
+      tc::tma_load_2d(sp + A_BYTES, &tal, x, m0, &full[s]);
+      tc::tma_load_2d(sp + 2 * A_BYTES, &tbh, x, n0, &full[s]);
+      tc::tma_load_2d(sp + 2 * A_BYTES + B_BYTES, &tbl, x, n0, &full[s]);
+    }
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
+    for (int kb = 0; kb < nk; kb++) {
+      const int s = kb % STAGES;
+      if (!tc::mbar_wait(&full[s], (kb / STAGES) & 1)) {
+        abort_flag = 1;
+        atomicOr(err, 2u);
+        break;
+      }
+      tc::fence_after();
+      const uint32_t ah = tc::smem_u32(smem + s * STAGE_BYTES), al = ah + A_BYTES;
+      const uint32_t bh = ah + 2 * A_BYTES, bl = bh + B_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; kk++) {
+        const uint32_t o = kk * 32;  // 16 bf16 = 32 bytes along K
+        tc::umma_bf16(tmem, tc::sdesc_sw128(ah + o), tc::sdesc_sw128(bh + o), idesc,
+                      (kb > 0 || kk > 0) ? 1u : 0u);
+        tc::umma_bf16(tmem, tc::sdesc_sw128(ah + o), tc::sdesc_sw128(bl + o), idesc, 1u);
+        tc::umma_bf16(tmem, tc::sdesc_sw128(al + o), tc::sdesc_sw128(bh + o), idesc, 1u);
+      }
+      tc::umma_commit(&empty[s]);
+    }
+    tc::umma_commit(&done);
+  }
+  __syncwarp();
+  const bool have = tc::mbar_wait(&done, 0);
+  if (!have && lane == 0) atomicOr(err, 4u);
+  // block-uniform: tcgen05.ld and the shuffles below are warp-collective
+  const bool drain = __syncthreads_and(have ? 1 : 0) && !abort_flag;
+  tc::fence_after();
+  if (drain) {
+    const int row = warp * 32 + lane;
+    const int c = (m0 + row) >> 1;
+    const bool odd = (lane & 1) != 0;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    float2 *o2 = reinterpret_cast<float2 *>(out) + ((size_t)blockIdx.z * C + c) * (size_t)ldo;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t r[32];
+      tc::tmem_ld32(tmem + lane_base + (uint32_t)c0, r);
+      // the even lane of a pair writes columns 0-15 of the chunk, the odd 16-31
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const float a0 = __uint_as_float(r[j]), a1 = __uint_as_float(r[16 + j]);
+        const float b0 = __shfl_xor_sync(0xffffffffu, a0, 1);
+        const float b1 = __shfl_xor_sync(0xffffffffu, a1, 1);
+        const int n = n0 + c0 + (odd ? 16 : 0) + j;
+        if (c < C && n < n_valid)
+          o2[n] = odd ? make_float2(b1, a1) : make_float2(a0, b0);
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem, (uint32_t)BN);
+  }
+}
+
+int round_up(long long v, int m) { return (int)((v + m - 1) / m * m); }
+
+// split of a k range of nkb blocks over enough CTAs for one wave
+void pick_split(int ntiles, int nkb, int sms, int &ks, int &kper) {
+  int want = std::max(1, (sms + ntiles - 1) / ntiles);
+  want = std::min(want, nkb);
+  kper = (nkb + want - 1) / want;
+  ks = (nkb + kper - 1) / kper;
+}
+
 }  // namespace
 
 ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
@@ -1028,6 +1263,156 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
   }
   switch (cbucket(a.C)) {
 #define CASE(CB) case CB: return run_cb<CB>(a, sp, M, Um, Ypart, G1, G2, part, counter, scal, GUp, gw, st);
+    CASE(1) CASE(2) CASE(4) CASE(8) CASE(16) CASE(32) CASE(64)
+#undef CASE
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// ------------------------------------------------------------------ plans
+struct ObjTcPlan {
+  const float *Hd, *Ha, *Hr;
+  int S, M, R, Cmax, K, Kp, Rp, Np, K2p, Mp;
+  int ksy, kpy, ksg, kpg;
+  __nv_bfloat16 *by_hi, *by_lo, *bg_hi, *bg_lo, *ay_hi, *ay_lo, *ag_hi, *ag_lo;
+  CUtensorMap m_byh, m_byl, m_bgh, m_bgl, m_ayh, m_ayl, m_agh, m_agl;
+  char *mem;      // one allocation: operands then scratch
+  size_t bytes;
+  size_t oCtl, oU, oY, oG1, oG2, oPart, oGU, oGw;  // byte offsets in mem
+};
+
+cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr, int S, int M,
+                               int R, int Cmax, cudaStream_t st, ObjTcPlan **out) {
+  *out = nullptr;
+  if (S <= 0 || M <= 0 || R <= 0 || Cmax <= 0 || Cmax > 64) return cudaErrorInvalidValue;
+  ObjTcPlan *p = new ObjTcPlan();
+  p->Hd = Hd; p->Ha = Ha; p->Hr = Hr;
+  p->S = S; p->M = M; p->R = R; p->Cmax = Cmax;
+  p->K = M + S;
+  p->Kp = round_up(2LL * p->K, 64);
+  p->Rp = round_up(R, tcg::BN);
+  p->Np = round_up(p->K, tcg::BN);
+  p->K2p = round_up(2LL * R, 64);
+  p->Mp = round_up(2LL * Cmax, tcg::BM);
+  const int sms = sm_count();
+  pick_split((p->Rp / tcg::BN) * (p->Mp / tcg::BM), p->Kp / tcg::BK, sms, p->ksy, p->kpy);
+  pick_split((p->Np / tcg::BN) * (p->Mp / tcg::BM), p->K2p / tcg::BK, sms, p->ksg, p->kpg);
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  size_t o = 0;
+  const size_t nby = (size_t)p->Rp * p->Kp, nbg = (size_t)p->Np * p->K2p;
+  const size_t nay = (size_t)p->Mp * p->Kp, nag = (size_t)p->Mp * p->K2p;
+  size_t oby = o; o += al(2 * nby) * 2;
+  size_t obg = o; o += al(2 * nbg) * 2;
+  size_t oay = o; o += al(2 * nay) * 2;
+  size_t oag = o; o += al(2 * nag) * 2;
+  p->oCtl = o;
+  o += kObjControlBytes;
+  p->oU = o; o += al(8 * (size_t)Cmax * M);
+  p->oY = o; o += al(8 * (size_t)p->ksy * Cmax * R);
+  p->oG1 = o; o += al(8 * (size_t)Cmax * R);
+  p->oG2 = o; o += al(8 * (size_t)Cmax * R);
+  p->oPart = o; o += al(16 * (size_t)((R + 127) / 128));
+  p->oGU = o; o += al(8 * (size_t)p->ksg * Cmax * p->K);
+  p->oGw = o; o += al(8 * (size_t)((M + 31) / 32) * Cmax * S);
+  p->bytes = o;
+  cudaError_t e = cudaMalloc(&p->mem, o);
+  if (e != cudaSuccess) { delete p; return e; }
+  p->by_hi = reinterpret_cast<__nv_bfloat16 *>(p->mem + oby);
+  p->by_lo = reinterpret_cast<__nv_bfloat16 *>(p->mem + oby + al(2 * nby));
+  p->bg_hi = reinterpret_cast<__nv_bfloat16 *>(p->mem + obg);
+  p->bg_lo = reinterpret_cast<__nv_bfloat16 *>(p->mem + obg + al(2 * nbg));
+  p->ay_hi = reinterpret_cast<__nv_bfloat16 *>(p->mem + oay);
+  p->ay_lo = reinterpret_cast<__nv_bfloat16 *>(p->mem + oay + al(2 * nay));
+  p->ag_hi = reinterpret_cast<__nv_bfloat16 *>(p->mem + oag);
+  p->ag_lo = reinterpret_cast<__nv_bfloat16 *>(p->mem + oag + al(2 * nag));
+  const bool ok =
+      tc::make_map_bf16(&p->m_byh, p->by_hi, p->Rp, p->Kp, tcg::BN) &&
+      tc::make_map_bf16(&p->m_byl, p->by_lo, p->Rp, p->Kp, tcg::BN) &&
+      tc::make_map_bf16(&p->m_bgh, p->bg_hi, p->Np, p->K2p, tcg::BN) &&
+      tc::make_map_bf16(&p->m_bgl, p->bg_lo, p->Np, p->K2p, tcg::BN) &&
+      tc::make_map_bf16(&p->m_ayh, p->ay_hi, p->Mp, p->Kp, tcg::BM) &&
+      tc::make_map_bf16(&p->m_ayl, p->ay_lo, p->Mp, p->Kp, tcg::BM) &&
+      tc::make_map_bf16(&p->m_agh, p->ag_hi, p->Mp, p->K2p, tcg::BM) &&
+      tc::make_map_bf16(&p->m_agl, p->ag_lo, p->Mp, p->K2p, tcg::BM);
+  if (!ok) { cudaFree(p->mem); delete p; return cudaErrorInvalidValue; }
+  static bool attr = false;
+  if (!attr) {
+    e = cudaFuncSetAttribute(k_cgemm3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)tcg::SMEM);
+    if (e != cudaSuccess) { cudaFree(p->mem); delete p; return e; }
+    attr = true;
+  }
+  // the A operands (rows beyond 2 C stay zero) and the control block
+  e = cudaMemsetAsync(p->mem + oay, 0, o - oay, st);
+  if (e == cudaSuccess) {
+    dim3 gb(p->Rp / 32, p->Kp / 64), bb(32, 8);
+    k_tc_make_by<<<gb, bb, 0, st>>>(Hr, Hd, M, S, R, p->Rp, p->Kp, p->by_hi, p->by_lo);
+    const long long ng = (long long)p->Np * (p->K2p / 2);
+    k_tc_make_bg<<<(unsigned)((ng + 255) / 256), 256, 0, st>>>(Hr, Hd, M, S, R, p->Np, p->K2p,
+                                                               p->bg_hi, p->bg_lo);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) { cudaFree(p->mem); delete p; return e; }
+  *out = p;
+  return cudaSuccess;
+}
+
+size_t obj_tc_plan_bytes(const ObjTcPlan *p) { return p ? p->bytes : 0; }
+
+void obj_tc_plan_destroy(ObjTcPlan *p) {
+  if (!p) return;
+  cudaFree(p->mem);
+  delete p;
+}
+
+namespace {
+template <int CB>
+cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
+  const int M = p->M, R = p->R, C = a.C;
+  float *U = reinterpret_cast<float *>(p->mem + p->oU);
+  float *Ypart = reinterpret_cast<float *>(p->mem + p->oY);
+  float *G1 = reinterpret_cast<float *>(p->mem + p->oG1);
+  float *G2 = C > 1 ? reinterpret_cast<float *>(p->mem + p->oG2) : nullptr;
+  double *part = reinterpret_cast<double *>(p->mem + p->oPart);
+  float *GUp = reinterpret_cast<float *>(p->mem + p->oGU);
+  float *gw = reinterpret_cast<float *>(p->mem + p->oGw);
+  float *scal = reinterpret_cast<float *>(ctl);
+  unsigned *counter = reinterpret_cast<unsigned *>(ctl + 32);
+  unsigned *err = reinterpret_cast<unsigned *>(ctl + 48);
+  k_prep<<<dim3((M + 127) / 128, C), 128, 0, st>>>(a, M, U);
+  const long long nay = (long long)C * (p->Kp / 2);
+  k_tc_make_ay<<<(unsigned)((nay + 255) / 256), 256, 0, st>>>(U, a.W, C, M, p->S, p->Kp,
+                                                              p->ay_hi, p->ay_lo);
+  dim3 gy(p->Rp / tcg::BN, p->Mp / tcg::BM, p->ksy);
+  k_cgemm3<<<gy, 128, tcg::SMEM, st>>>(p->m_ayh, p->m_ayl, p->m_byh, p->m_byl, p->kpy,
+                                        p->Kp / tcg::BK, C, R, R, Ypart, err);
+  k_epilogue<CB><<<(R + 127) / 128, 128, 0, st>>>(a, p->ksy, Ypart, G1, G2, part, counter, scal);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (a.grad_Y) {
+    const long long n = (long long)C * R;
+    k_grad_y<<<(int)((n + 255) / 256), 256, 0, st>>>(G1, G2, scal, n, a.grad_Y);
+  }
+  if (!a.grad_W && !a.grad_phi) return cudaGetLastError();
+  const long long nag = (long long)C * (p->K2p / 2);
+  k_tc_make_ag<<<(unsigned)((nag + 255) / 256), 256, 0, st>>>(G1, G2, scal, C, R, p->K2p,
+                                                              p->ag_hi, p->ag_lo);
+  dim3 gg(p->Np / tcg::BN, p->Mp / tcg::BM, p->ksg);
+  k_cgemm3<<<gg, 128, tcg::SMEM, st>>>(p->m_agh, p->m_agl, p->m_bgh, p->m_bgl, p->kpg,
+                                        p->K2p / tcg::BK, C, p->K, p->K, GUp, err);
+  k_final<CB><<<(M + 31) / 32, 256, 0, st>>>(a, M, p->K, p->ksg, U, GUp, gw, counter + 1);
+  return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t obj_tc_run(ObjTcPlan *p, const ObjArgs &a0, cudaStream_t st) {
+  if (!p || a0.C <= 0 || a0.C > p->Cmax) return cudaErrorInvalidValue;
+  ObjArgs a = a0;
+  a.Hd = p->Hd; a.Ha = p->Ha; a.Hr = p->Hr;
+  a.S = p->S; a.M = p->M; a.R = p->R;
+  char *ctl = p->mem + p->oCtl;
+  switch (cbucket(a.C)) {
+#define CASE(CB) case CB: return run_tc<CB>(p, a, ctl, st);
     CASE(1) CASE(2) CASE(4) CASE(8) CASE(16) CASE(32) CASE(64)
 #undef CASE
     default: return cudaErrorInvalidValue;

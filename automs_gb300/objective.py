@@ -30,13 +30,50 @@ def _c64(t):
     return t if t.is_contiguous() else t.contiguous()
 
 
+class ObjectivePlan:
+    """Tensor-core objective for a fixed channel set (ams_objective_plan_*).
+
+    [H_r; H_d] are converted once into BF16 hi/lo pairs; each evaluation then
+    runs the forward and adjoint contractions as tcgen05 GEMMs (3xBF16
+    products, FP32 accumulation, relative error about 1e-5).  For codebooks
+    (C up to c_max <= 64) evaluated many times, as in optimize_model."""
+
+    def __init__(self, H_d, H_a, H_r, c_max=64):
+        lib()
+        self.Hd, self.Ha, self.Hr = _c64(H_d.detach()), _c64(H_a.detach()), _c64(H_r.detach())
+        self.S, self.R = self.Hd.shape
+        self.M = self.Ha.shape[1]
+        if self.Ha.shape[0] != self.S or tuple(self.Hr.shape) != (self.M, self.R):
+            raise ValueError("channel shapes do not match: H_d [S,R], H_a [S,M], H_r [M,R]")
+        self.c_max = int(c_max)
+        h = C.c_void_p()
+        call("ams_objective_plan_create", _ptr(self.Hd), _ptr(self.Ha), _ptr(self.Hr), self.S,
+             self.M, self.R, self.c_max, _stream(), C.byref(h))
+        self._h = h
+
+    @property
+    def nbytes(self):
+        return int(lib().ams_objective_plan_bytes(self._h)) if self._h else 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ams_objective_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class CapacityObjective(torch.autograd.Function):
     """loss(W, phi) of go.py:159-226 for one metasurface hop (or none):
     Y = W H_d + ((W H_a) o e^{j (phi mod max_phase)}) H_r.
     The adjoint is computed in the same call; backward only scales it."""
 
     @staticmethod
-    def forward(ctx, W, phi, H_d, H_a, H_r, max_phase, w, drop, want_recv):
+    def forward(ctx, W, phi, H_d, H_a, H_r, max_phase, w, drop, want_recv, plan=None):
         Cc, S = W.shape
         R = H_d.shape[1]
         ms = H_a is not None
@@ -53,9 +90,16 @@ class CapacityObjective(torch.autograd.Function):
         gY = torch.empty(Cc, R, dtype=torch.complex64, device=W.device) if need_gy else None
         recv = torch.empty(Cc, R, dtype=torch.float32, device=W.device) if want_recv else None
         dr = drop.to(device=W.device, dtype=torch.uint8).contiguous() if drop is not None else None
-        call("ams_objective_fwd_bwd", _ptr(Hd), _ptr(Ha), _ptr(Hr), _ptr(ph), float(max_phase),
-             _ptr(Wc), S, M, R, Cc, float(w), _ptr(dr), _ptr(loss), _ptr(gW), _ptr(gphi),
-             _ptr(gY), _ptr(recv), _stream())
+        if plan is not None:
+            if not ms or (plan.S, plan.M, plan.R) != (S, M, R):
+                raise ValueError("the plan was made for other channel shapes")
+            call("ams_objective_plan_fwd_bwd", plan._h, _ptr(ph), float(max_phase), _ptr(Wc), Cc,
+                 float(w), _ptr(dr), _ptr(loss), _ptr(gW), _ptr(gphi), _ptr(gY), _ptr(recv),
+                 _stream())
+        else:
+            call("ams_objective_fwd_bwd", _ptr(Hd), _ptr(Ha), _ptr(Hr), _ptr(ph),
+                 float(max_phase), _ptr(Wc), S, M, R, Cc, float(w), _ptr(dr), _ptr(loss),
+                 _ptr(gW), _ptr(gphi), _ptr(gY), _ptr(recv), _stream())
         ctx.save_for_backward(gW, gphi if gphi is not None else torch.empty(0, device=W.device),
                               gY if gY is not None else torch.empty(0, device=W.device), Wc)
         ctx.ms = ms
@@ -75,15 +119,17 @@ class CapacityObjective(torch.autograd.Function):
         if ctx.need_gy and ctx.needs_input_grad[2]:
             # Y = W H_d  =>  dL/dH_d = W^H dL/dY (torch's complex convention)
             dHd = (Wc.conj().transpose(0, 1) @ gY) * gl
-        return dW, dphi, dHd, None, None, None, None, None, None
+        return dW, dphi, dHd, None, None, None, None, None, None, None
 
 
 def capacity_objective(W, H_d, H_a=None, H_r=None, phi=None, max_phase=2 * math.pi, w=1.0,
-                       drop=None, return_recv=False):
+                       drop=None, return_recv=False, plan=None):
     """Differentiable objective.  W [C,S] complex, H_d [S,R], H_a [S,M],
-    H_r [M,R] complex64 CUDA tensors, phi [M] float, drop [C] bool."""
+    H_r [M,R] complex64 CUDA tensors, phi [M] float, drop [C] bool.  With an
+    ObjectivePlan made from these channels the tensor-core path runs."""
     lib()
-    loss, recv = CapacityObjective.apply(W, phi, H_d, H_a, H_r, max_phase, w, drop, return_recv)
+    loss, recv = CapacityObjective.apply(W, phi, H_d, H_a, H_r, max_phase, w, drop, return_recv,
+                                         plan)
     return (loss, recv) if return_recv else loss
 
 

@@ -132,3 +132,98 @@ def test_coverage_db(obj):
     ref = 20 * np.log10(np.abs(H.sum(0).astype(np.complex128)))
     ref = np.maximum(np.where(np.isnan(ref), -150.0, ref), -150.0)
     np.testing.assert_allclose(out, ref, atol=1e-4)
+
+
+def _tc_inputs(c, C=None):
+    ch = c["channels"]
+    Cc = c["code_num"] if C is None else C
+    theta = c["theta"][:Cc]
+    A = OO.antenna_amplitude(Cc, theta.shape[1])
+    drop = np.zeros(Cc, bool)
+    if Cc > 2:
+        drop[1] = True
+    mp = c["max_phase_deg"] / 180 * np.pi
+    return ch, theta, A, drop, mp
+
+
+def _cfg1_codes(C=60, seed=7):
+    """S=16 AP, 32x32 metasurface, 64x64 Rx with a C-code codebook."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    S, M, R = 16, 1024, 4096
+    ch = {"src_to_dst": cases._cn(rng, (S, R)), "src_to_ms{0}": cases._cn(rng, (S, M)),
+          "ms{0}_to_dst": cases._cn(rng, (M, R))}
+    return dict(channels=ch, theta=rng.uniform(0, 2 * np.pi, size=(C, S)).astype(np.float32),
+                phi=[rng.uniform(0, 2 * np.pi, size=M).astype(np.float32)], n_ms=1,
+                code_num=C, w=1.0 / R, max_phase_deg=360.0)
+
+
+@pytest.mark.parametrize("name", ["c1", "c30", "cfg1_c60"])
+def test_tensor_core_plan_vs_oracle(obj, name):
+    """Tensor-core (3xBF16, FP32 accumulation) evaluation against the FP64
+    oracle: loss and |Y| to 1e-4 relative, gradients to 1e-3 of their scale
+    (the 3xBF16 products carry about 1e-5 relative error)."""
+    c = _cfg1_codes() if name == "cfg1_c60" else cases.objective_case(name)
+    ch, theta_np, A, drop, mp = _tc_inputs(c)
+    Hd, Ha, Hr = ch["src_to_dst"], ch["src_to_ms{0}"], ch["ms{0}_to_dst"]
+    phi = c["phi"][0]
+    loss_o, gth_o, gphi_o, ex = OO.objective(Hd, Ha, Hr, phi, theta_np, A, c["w"], drop, mp)
+    plan = obj.ObjectivePlan(cuda(Hd), cuda(Ha), cuda(Hr), c_max=64)
+    theta = cuda(theta_np).requires_grad_(True)
+    W = cuda(A.astype(np.float32)) * torch.exp(-1j * theta)
+    ph = cuda(phi).requires_grad_(True)
+    loss, recv = obj.capacity_objective(W, cuda(Hd), cuda(Ha), cuda(Hr), ph, mp, c["w"],
+                                        cuda(drop), return_recv=True, plan=plan)
+    loss.backward()
+    np.testing.assert_allclose(float(loss), loss_o, rtol=1e-4)
+    np.testing.assert_allclose(recv.cpu().numpy(), ex["amp"], rtol=1e-4,
+                               atol=1e-4 * np.abs(ex["amp"]).max())
+    g = theta.grad.cpu().numpy()
+    np.testing.assert_allclose(g, gth_o, rtol=1e-3, atol=1e-3 * np.abs(gth_o).max())
+    gp = ph.grad.cpu().numpy()
+    np.testing.assert_allclose(gp, gphi_o, rtol=1e-3, atol=1e-3 * np.abs(gphi_o).max())
+    plan.close()
+
+
+def test_tensor_core_plan_matches_cuda_core_path(obj):
+    """Same evaluation on the plan and on the FP32 CUDA-core path, the plan
+    reused across calls with different C, phi and dropout."""
+    c = _cfg1_codes(C=48, seed=11)
+    ch = c["channels"]
+    Hd, Ha, Hr = (cuda(ch[k]) for k in ("src_to_dst", "src_to_ms{0}", "ms{0}_to_dst"))
+    plan = obj.ObjectivePlan(Hd, Ha, Hr, c_max=48)
+    assert plan.nbytes > 0
+    rng = np.random.Generator(np.random.PCG64(5))
+    for C in (48, 5, 1, 33):
+        th = cuda(rng.uniform(0, 2 * np.pi, size=(C, 16)).astype(np.float32))
+        W = torch.exp(-1j * th)
+        phi = cuda(rng.uniform(0, 2 * np.pi, size=1024).astype(np.float32))
+        drop = cuda(rng.random(C) < 0.2)
+        outs = []
+        for p in (plan, None):
+            Wg = W.clone().requires_grad_(True)
+            pg = phi.clone().requires_grad_(True)
+            loss, recv = obj.capacity_objective(Wg, Hd, Ha, Hr, pg, 2 * np.pi, 0.5, drop,
+                                                return_recv=True, plan=p)
+            loss.backward()
+            outs.append((float(loss), recv, Wg.grad, pg.grad))
+        (l1, r1, w1, p1), (l2, r2, w2, p2) = outs
+        assert abs(l1 - l2) <= 1e-4 * abs(l2)
+        assert torch.allclose(r1, r2, rtol=1e-4, atol=1e-4 * float(r2.abs().max()))
+        assert float((w1 - w2).abs().max()) <= 1e-3 * float(w2.abs().max())
+        assert float((p1 - p2).abs().max()) <= 1e-3 * float(p2.abs().max())
+    plan.close()
+
+
+def test_tensor_core_plan_errors(obj):
+    from automs_gb300._lib import AmsError
+    c = cases.objective_case("c30")
+    ch = c["channels"]
+    Hd, Ha, Hr = (cuda(ch[k]) for k in ("src_to_dst", "src_to_ms{0}", "ms{0}_to_dst"))
+    with pytest.raises(AmsError):
+        obj.ObjectivePlan(Hd, Ha, Hr, c_max=65)
+    plan = obj.ObjectivePlan(Hd, Ha, Hr, c_max=8)
+    W = torch.ones(9, Hd.shape[0], dtype=torch.complex64, device="cuda")
+    phi = torch.zeros(Ha.shape[1], device="cuda")
+    with pytest.raises(AmsError):
+        obj.capacity_objective(W, Hd, Ha, Hr, phi, plan=plan)
+    plan.close()
