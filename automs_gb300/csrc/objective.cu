@@ -59,6 +59,21 @@ __device__ __forceinline__ float py_mod(float a, float b) {
   return r;
 }
 
+// x = hi + lo with hi = bf16(x), lo = bf16(x - hi); a pair of values goes to
+// element `pair` of the bf16x2 views of the hi and lo arrays
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
+  hi = __float2bfloat16_rn(x);
+  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+__device__ __forceinline__ void put_pair(__nv_bfloat16 *hi, __nv_bfloat16 *lo, size_t pair,
+                                         float a, float b) {
+  __nv_bfloat16 h0, l0, h1, l1;
+  split_bf16(a, h0, l0);
+  split_bf16(b, h1, l1);
+  reinterpret_cast<__nv_bfloat162 *>(hi)[pair] = __halves2bfloat162(h0, h1);
+  reinterpret_cast<__nv_bfloat162 *>(lo)[pair] = __halves2bfloat162(l0, l1);
+}
+
 // ------------------------------------------------------------------
 // Virtual rows k in [0, K), K = M + S: row k < M is H_r[k, :] with
 // coefficient U[c, k]; row k >= M is H_d[k - M, :] with coefficient
@@ -191,6 +206,32 @@ __global__ void __launch_bounds__(256) k_pass1(ObjArgs a, int M, int K, int kper
   }
 }
 
+// Sum of the CTAs' (sum_max, sum_sq) pairs by every thread of the last CTA
+// (FP64 adds have a long latency on this part; one thread alone would chain
+// thousands of them).  Reads bypass L1: the pairs were written by other CTAs.
+// The result is valid in thread 0; all threads of the block must call it.
+__device__ __forceinline__ void block_sum_pairs(const double *partials, int nb, double &x,
+                                                double &z) {
+  __threadfence();
+  double px = 0.0, pz = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    px += __ldcg(partials + 2 * b);
+    pz += __ldcg(partials + 2 * b + 1);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    px += __shfl_xor_sync(0xffffffffu, px, o);
+    pz += __shfl_xor_sync(0xffffffffu, pz, o);
+  }
+  __shared__ double red[2][32];
+  const int wid = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { red[0][wid] = px; red[1][wid] = pz; }
+  __syncthreads();
+  x = 0.0;
+  z = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++) { x += red[0][i]; z += red[1][i]; }
+}
+
 // epilogue: Y from the partials, per-Rx capacity / dropout / max / mask and
 // the gradient parts; the last CTA reduces the block sums into the loss.
 template <int CB>
@@ -198,7 +239,7 @@ __global__ void __launch_bounds__(256) k_epilogue(ObjArgs a, int kspl, const flo
                                                   float *G1, float *G2, double *partials,
                                                   unsigned *counter, float *scal) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  double sum_max = 0.0, sum_sq = 0.0;
+  float sum_max = 0.f, sum_sq = 0.f;  // FP32 within a warp, FP64 across warps
   if (r < a.R) {
     c2 y[CB];
     float cap[CB], amp[CB];
@@ -235,7 +276,7 @@ __global__ void __launch_bounds__(256) k_epilogue(ObjArgs a, int kspl, const flo
       if (c >= a.C) continue;
       const bool dropped = a.drop && a.drop[c];
       const float msk = (cap[c] != mx) ? cap[c] : 0.f;  // cap' * mask
-      sum_sq += (double)msk * msk;
+      sum_sq += msk * msk;
       const float aa = amp[c] + kEps;
       const float dcap = (2.0f * aa / kN0) / (1.0f + aa * aa / kN0) * kInvLn2;
       float g1 = (c == arg) ? -a.w : 0.f, g2 = msk;
@@ -266,16 +307,286 @@ __global__ void __launch_bounds__(256) k_epilogue(ObjArgs a, int kspl, const flo
     last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double x = 0, z = 0;
-    const volatile double *pp = partials;
-    for (int b = 0; b < (int)gridDim.x; b++) { x += pp[2 * b]; z += pp[2 * b + 1]; }
-    const double nrm = sqrt(z);
-    if (a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
-    scal[0] = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
-    *counter = 0u;  // ready for the next call
+  if (last) {
+    double x, z;
+    block_sum_pairs(partials, (int)gridDim.x, x, z);
+    if (threadIdx.x == 0) {
+      const double nrm = sqrt(z);
+      if (a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
+      scal[0] = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+      *counter = 0u;  // ready for the next call
+    }
   }
+}
+
+// epilogue for codebooks (CB >= 8): a CTA takes 32 Rx (one per lane) and
+// its 8 warps split the codes (warp w: c = w, w + 8, ...), so a thread keeps
+// CB / 8 codes.  The max over codes (first index on ties) is reduced across
+// the warps in shared memory; then each thread writes its codes' gradient
+// parts.  Loss partials and the last-CTA reduction as in k_epilogue.
+template <int CB>
+__global__ void __launch_bounds__(256) k_epilogue_wide(ObjArgs a, int kspl, const float *Ypart,
+                                                       float *G1, float *G2, double *partials,
+                                                       unsigned *counter, float *scal) {
+  constexpr int CPT = CB / 8;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int r = blockIdx.x * 32 + lane;
+  const bool live = r < a.R;
+  c2 y[CPT];
+  float amp[CPT], cap[CPT];
+  float mx = -1.f;
+  int arg = 0x7fffffff;
+  // all loads first (independent across codes), then the arithmetic
+  const int rr = live ? r : 0;
+  for (int sp = 0; sp < kspl; sp++) {
+    c2 v[CPT];
+#pragma unroll
+    for (int j = 0; j < CPT; j++) {
+      const int c = min(wid + 8 * j, a.C - 1);
+      v[j] = ld2(Ypart, ((size_t)sp * a.C + c) * a.R + rr);
+    }
+#pragma unroll
+    for (int j = 0; j < CPT; j++) {
+      if (sp == 0) y[j] = v[j];
+      else { y[j].x += v[j].x; y[j].y += v[j].y; }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < CPT; j++) {
+    const int c = wid + 8 * j;
+    amp[j] = 0.f;
+    cap[j] = 0.f;
+    if (!live || c >= a.C) continue;
+    amp[j] = sqrtf(y[j].x * y[j].x + y[j].y * y[j].y);
+    const float aa = amp[j] + kEps;
+    float v = log2f(1.0f + aa * aa / kN0);
+    if (a.drop && a.drop[c]) v = 0.f;
+    cap[j] = v;
+    if (v > mx) { mx = v; arg = c; }  // codes ascend within a thread
+    if (a.recv_amp) a.recv_amp[(size_t)c * a.R + r] = amp[j];
+  }
+  __shared__ float smx[8][32];
+  __shared__ int sarg[8][32];
+  smx[wid][lane] = mx;
+  sarg[wid][lane] = arg;
+  __syncthreads();
+  float M_ = smx[0][lane];
+  int A_ = sarg[0][lane];
+#pragma unroll
+  for (int w2 = 1; w2 < 8; w2++) {
+    const float v = smx[w2][lane];
+    const int g = sarg[w2][lane];
+    if (v > M_ || (v == M_ && g < A_)) { M_ = v; A_ = g; }
+  }
+  // FP32 within a warp (FP64 arithmetic is slow here), FP64 across warps
+  float sum_max = (live && wid == 0) ? M_ : 0.f, sum_sq = 0.f;
+#pragma unroll
+  for (int j = 0; j < CPT; j++) {
+    const int c = wid + 8 * j;
+    if (!live || c >= a.C) continue;
+    const bool dropped = a.drop && a.drop[c];
+    const float msk = (cap[j] != M_) ? cap[j] : 0.f;
+    sum_sq += msk * msk;
+    const float aa = amp[j] + kEps;
+    const float dcap = (2.0f * aa / kN0) / (1.0f + aa * aa / kN0) * kInvLn2;
+    float g1 = (c == A_) ? -a.w : 0.f, g2 = msk;
+    if (dropped) { g1 = 0.f; g2 = 0.f; }
+    const float sc = amp[j] > 0.f ? dcap / amp[j] : 0.f;
+    reinterpret_cast<float2 *>(G1)[(size_t)c * a.R + r] =
+        make_float2(g1 * sc * y[j].x, g1 * sc * y[j].y);
+    if (G2)
+      reinterpret_cast<float2 *>(G2)[(size_t)c * a.R + r] =
+          make_float2(g2 * sc * y[j].x, g2 * sc * y[j].y);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sum_max += __shfl_xor_sync(0xffffffffu, sum_max, o);
+    sum_sq += __shfl_xor_sync(0xffffffffu, sum_sq, o);
+  }
+  __shared__ double spart[2][8];
+  __shared__ bool last;
+  if (lane == 0) { spart[0][wid] = sum_max; spart[1][wid] = sum_sq; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0, z = 0;
+    for (int i = 0; i < 8; i++) { x += spart[0][i]; z += spart[1][i]; }
+    partials[2 * blockIdx.x] = x;
+    partials[2 * blockIdx.x + 1] = z;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) {
+    double x, z;
+    block_sum_pairs(partials, (int)gridDim.x, x, z);
+    if (threadIdx.x == 0) {
+      const double nrm = sqrt(z);
+      if (a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
+      scal[0] = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+      *counter = 0u;  // ready for the next call
+    }
+  }
+}
+
+// Two-phase epilogue of the tensor-core path (CB >= 8), same thread layout
+// as k_epilogue_wide.  Phase A: loss partials, and per Rx the max over codes
+// and its first index.  Phase B: re-reads Y, forms G = G1 + G2 / ||masked||
+// and writes it straight into the A operand of the adjoint GEMM (and
+// grad_Y), so G1 / G2 are never stored.  Both phases evaluate the capacity
+// with the same inline code, so they see bit-identical values.
+template <int CPT>
+__device__ __forceinline__ void epi_load_y(const ObjArgs &a, int kspl, const float *Ypart, int wid,
+                                           int rr, c2 (&y)[CPT]) {
+  for (int sp = 0; sp < kspl; sp++) {
+    c2 v[CPT];
+#pragma unroll
+    for (int j = 0; j < CPT; j++) {
+      const int c = min(wid + 8 * j, a.C - 1);
+      v[j] = ld2(Ypart, ((size_t)sp * a.C + c) * a.R + rr);
+    }
+#pragma unroll
+    for (int j = 0; j < CPT; j++) {
+      if (sp == 0) y[j] = v[j];
+      else { y[j].x += v[j].x; y[j].y += v[j].y; }
+    }
+  }
+}
+__device__ __forceinline__ void epi_cap(const ObjArgs &a, int c, c2 y, float &amp, float &cap) {
+  amp = sqrtf(y.x * y.x + y.y * y.y);
+  const float aa = amp + kEps;
+  float v = log2f(1.0f + aa * aa / kN0);
+  if (a.drop && a.drop[c]) v = 0.f;
+  cap = v;
+}
+
+template <int CB>
+__global__ void __launch_bounds__(256) k_tc_epi_a(ObjArgs a, int kspl, const float *Ypart,
+                                                  float *maxr, int *argr, double *partials,
+                                                  unsigned *counter, float *scal) {
+  constexpr int CPT = CB / 8;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int r = blockIdx.x * 32 + lane;
+  const bool live = r < a.R;
+  c2 y[CPT];
+  float cap[CPT];
+  epi_load_y<CPT>(a, kspl, Ypart, wid, live ? r : 0, y);
+  float mx = -1.f;
+  int arg = 0x7fffffff;
+#pragma unroll
+  for (int j = 0; j < CPT; j++) {
+    const int c = wid + 8 * j;
+    cap[j] = 0.f;
+    if (!live || c >= a.C) continue;
+    float amp;
+    epi_cap(a, c, y[j], amp, cap[j]);
+    if (cap[j] > mx) { mx = cap[j]; arg = c; }
+    if (a.recv_amp) a.recv_amp[(size_t)c * a.R + r] = amp;
+  }
+  __shared__ float smx[8][32];
+  __shared__ int sarg[8][32];
+  smx[wid][lane] = mx;
+  sarg[wid][lane] = arg;
+  __syncthreads();
+  float M_ = smx[0][lane];
+  int A_ = sarg[0][lane];
+#pragma unroll
+  for (int w2 = 1; w2 < 8; w2++) {
+    const float v = smx[w2][lane];
+    const int g = sarg[w2][lane];
+    if (v > M_ || (v == M_ && g < A_)) { M_ = v; A_ = g; }
+  }
+  if (wid == 0 && live) { maxr[r] = M_; argr[r] = A_; }
+  // FP32 within a warp (FP64 arithmetic is slow here), FP64 across warps
+  float sum_max = (live && wid == 0) ? M_ : 0.f, sum_sq = 0.f;
+#pragma unroll
+  for (int j = 0; j < CPT; j++) {
+    const int c = wid + 8 * j;
+    if (!live || c >= a.C) continue;
+    const float msk = (cap[j] != M_) ? cap[j] : 0.f;
+    sum_sq += msk * msk;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sum_max += __shfl_xor_sync(0xffffffffu, sum_max, o);
+    sum_sq += __shfl_xor_sync(0xffffffffu, sum_sq, o);
+  }
+  __shared__ double spart[2][8];
+  __shared__ bool last;
+  if (lane == 0) { spart[0][wid] = sum_max; spart[1][wid] = sum_sq; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0, z = 0;
+    for (int i = 0; i < 8; i++) { x += spart[0][i]; z += spart[1][i]; }
+    partials[2 * blockIdx.x] = x;
+    partials[2 * blockIdx.x + 1] = z;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) {
+    double x, z;
+    block_sum_pairs(partials, (int)gridDim.x, x, z);
+    if (threadIdx.x == 0) {
+      const double nrm = sqrt(z);
+      if (a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
+      scal[0] = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+      *counter = 0u;  // ready for the next call
+    }
+  }
+}
+
+template <int CB>
+__global__ void __launch_bounds__(256) k_tc_epi_b(ObjArgs a, int kspl, const float *Ypart,
+                                                  const float *maxr, const int *argr,
+                                                  const float *scal, int K2p, __nv_bfloat16 *hi,
+                                                  __nv_bfloat16 *lo) {
+  constexpr int CPT = CB / 8;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int r = blockIdx.x * 32 + lane;
+  const bool live = r < a.R;
+  c2 y[CPT];
+  epi_load_y<CPT>(a, kspl, Ypart, wid, live ? r : 0, y);
+  const float M_ = live ? maxr[r] : 0.f;
+  const int A_ = live ? argr[r] : 0;
+  const float inv = a.C > 1 ? scal[0] : 0.f;
+#pragma unroll
+  for (int j = 0; j < CPT; j++) {
+    const int c = wid + 8 * j;
+    if (c >= a.C) continue;
+    c2 g = {0.f, 0.f};
+    if (live) {
+      float amp, cap;
+      epi_cap(a, c, y[j], amp, cap);
+      const bool dropped = a.drop && a.drop[c];
+      const float msk = (cap != M_) ? cap : 0.f;
+      const float aa = amp + kEps;
+      const float dcap = (2.0f * aa / kN0) / (1.0f + aa * aa / kN0) * kInvLn2;
+      float g1 = (c == A_) ? -a.w : 0.f, g2 = msk;
+      if (dropped) { g1 = 0.f; g2 = 0.f; }
+      const float sc = amp > 0.f ? dcap / amp : 0.f;
+      // G1 + G2 * inv with the rounding of k_tc_make_ag: fmaf(G2, inv, G1)
+      const c2 q1 = {g1 * sc * y[j].x, g1 * sc * y[j].y};
+      const c2 q2 = {g2 * sc * y[j].x, g2 * sc * y[j].y};
+      g.x = fmaf(q2.x, inv, q1.x);
+      g.y = fmaf(q2.y, inv, q1.y);
+      if (a.grad_Y) reinterpret_cast<float2 *>(a.grad_Y)[(size_t)c * a.R + r] = make_float2(g.x, g.y);
+    }
+    if (r < K2p / 2) {
+      put_pair(hi, lo, ((size_t)(2 * c) * K2p + 2 * r) / 2, g.x, g.y);
+      put_pair(hi, lo, ((size_t)(2 * c + 1) * K2p + 2 * r) / 2, g.y, -g.x);
+    }
+  }
+}
+
+// G_U[c, k] = sum over the splits of the partials, one thread per entry
+__global__ void k_gu_reduce(const float *GUp, int splits, long long n, float *GU) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float x = 0.f, y = 0.f;
+  for (int s = 0; s < splits; s++) {
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(GUp) + (size_t)s * n + i);
+    x += v.x;
+    y += v.y;
+  }
+  reinterpret_cast<float2 *>(GU)[i] = make_float2(x, y);
 }
 
 // pass 2: partial G_U[c, k] = sum_r G[c, r] conj(row_k[r]) over an r-range;
@@ -414,6 +725,92 @@ __global__ void __launch_bounds__(256) k_final(ObjArgs a, int M, int K, int rspl
   if (t == 0) *counter = 0u;  // ready for the next call
 }
 
+// dphi[m] = -sum_c Im(conj(G_U[c, m]) U[c, m]); a CTA takes 32 elements
+// (lanes) and its 8 warps split the codes
+__global__ void __launch_bounds__(256) k_tc_dphi(const float *GU, const float *U, int C, int M,
+                                                 int K, float *dphi) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int m = blockIdx.x * 32 + lane;
+  float acc = 0.f;
+  if (m < M)
+    for (int c = wid; c < C; c += 8) {
+      const float2 g = __ldg(reinterpret_cast<const float2 *>(GU) + (size_t)c * K + m);
+      const float2 u = __ldg(reinterpret_cast<const float2 *>(U) + (size_t)c * M + m);
+      acc += g.x * u.y - g.y * u.x;
+    }
+  __shared__ float red[8][32];
+  red[wid][lane] = acc;
+  __syncthreads();
+  if (wid == 0 && m < M) {
+    float t = 0.f;
+#pragma unroll
+    for (int w2 = 0; w2 < 8; w2++) t += red[w2][lane];
+    dphi[m] = -t;
+  }
+}
+
+// grad_W[c, s] = G_U[c, M + s] + sum_m G_U[c, m] e^{-j phi'_m} conj(H_a[s, m]).
+// k_tc_dw_part: CTA (c, part) takes a slice of the m range, one element per
+// thread, keeps 16 AP elements' sums at a time in registers (H_a loads
+// coalesced over m) and writes the CTA's sums to dwp[c][part][s];
+// k_tc_dw_sum adds the slices and the H_d term.
+constexpr int kDwParts = 8;
+__global__ void __launch_bounds__(128) k_tc_dw_part(const float *GU, const float *Ha,
+                                                    const float *phi, float max_phase, int S,
+                                                    int M, int K, float *dwp) {
+  constexpr int SB = 16;
+  __shared__ float2 red[4][SB];
+  const int c = blockIdx.x, part = blockIdx.y;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int per = (M + kDwParts - 1) / kDwParts;
+  const int m_lo = part * per, m_hi = min(M, m_lo + per);
+  for (int s0 = 0; s0 < S; s0 += SB) {
+    c2 acc[SB];
+#pragma unroll
+    for (int q = 0; q < SB; q++) acc[q] = {0.f, 0.f};
+    for (int m = m_lo + threadIdx.x; m < m_hi; m += blockDim.x) {
+      const float2 g = __ldg(reinterpret_cast<const float2 *>(GU) + (size_t)c * K + m);
+      float sn, cs;
+      sincosf(py_mod(__ldg(phi + m), max_phase), &sn, &cs);
+      const c2 ge = {g.x * cs + g.y * sn, g.y * cs - g.x * sn};  // g e^{-j p}
+#pragma unroll
+      for (int q = 0; q < SB; q++)
+        if (s0 + q < S) macc(acc[q], ge, ld2(Ha, (size_t)(s0 + q) * M + m));
+    }
+#pragma unroll
+    for (int q = 0; q < SB; q++) {
+      float x = acc[q].x, y = acc[q].y;
+      for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+        y += __shfl_xor_sync(0xffffffffu, y, o);
+      }
+      if (lane == 0) red[wid][q] = make_float2(x, y);
+    }
+    __syncthreads();
+    if (threadIdx.x < SB && s0 + threadIdx.x < S) {
+      float2 t = red[0][threadIdx.x];
+#pragma unroll
+      for (int w2 = 1; w2 < 4; w2++) { t.x += red[w2][threadIdx.x].x; t.y += red[w2][threadIdx.x].y; }
+      reinterpret_cast<float2 *>(dwp)[((size_t)c * kDwParts + part) * S + s0 + threadIdx.x] = t;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_tc_dw_sum(const float *GU, const float *dwp, int C, int S, int M, int K,
+                            float *grad_W) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= C * S) return;
+  const int c = i / S, s2 = i % S;
+  float2 t = __ldg(reinterpret_cast<const float2 *>(GU) + (size_t)c * K + M + s2);
+  for (int q = 0; q < kDwParts; q++) {
+    const float2 v = reinterpret_cast<const float2 *>(dwp)[((size_t)c * kDwParts + q) * S + s2];
+    t.x += v.x;
+    t.y += v.y;
+  }
+  reinterpret_cast<float2 *>(grad_W)[i] = t;
+}
+
 // grad_Y = G1 + G2 / ||masked||
 __global__ void k_grad_y(const float *G1, const float *G2, const float *scal, long long n,
                          float *out) {
@@ -466,7 +863,11 @@ cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *U, float *Yp
   }
   dim3 g1((a.R + 31) / 32, sp.kspl);
   k_pass1<CB><<<g1, 256, 0, st>>>(a, M, sp.K, sp.kper, U, Ypart);
-  k_epilogue<CB><<<sp.nb_epi, 128, 0, st>>>(a, sp.kspl, Ypart, G1, G2, part, counter, scal);
+  if (CB >= 8)
+    k_epilogue_wide<(CB >= 8 ? CB : 8)><<<(a.R + 31) / 32, 256, 0, st>>>(a, sp.kspl, Ypart, G1,
+                                                                        G2, part, counter, scal);
+  else
+    k_epilogue<CB><<<sp.nb_epi, 128, 0, st>>>(a, sp.kspl, Ypart, G1, G2, part, counter, scal);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (a.grad_Y) {
@@ -580,7 +981,7 @@ __global__ void __launch_bounds__(256, 2)
   for (int q = 0; q < KPT; q++)
 #pragma unroll
     for (int c = 0; c < CB; c++) { p1[q][c] = {0.f, 0.f}; p2[q][c] = {0.f, 0.f}; }
-  double sum_max = 0.0, sum_sq = 0.0;
+  float sum_max = 0.f, sum_sq = 0.f;  // FP32 within a warp, FP64 across warps
   const int col = t % TR, j = t / TR;
   constexpr int NJ = NTH / TR;
 
@@ -646,7 +1047,7 @@ __global__ void __launch_bounds__(256, 2)
         if (c < a.C && r < a.R) {
           const bool dropped = a.drop && a.drop[c];
           const float msk = (cap[c] != mx) ? cap[c] : 0.f;
-          sum_sq += (double)msk * msk;
+          sum_sq += msk * msk;
           const float aa = amp[c] + kEps;
           const float dcap = (2.0f * aa / kN0) / (1.0f + aa * aa / kN0) * kInvLn2;
           float g1 = (c == arg) ? -a.w : 0.f, g2 = msk;
@@ -1004,18 +1405,6 @@ constexpr uint32_t STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
 constexpr size_t SMEM = STAGES * STAGE_BYTES + 1024;
 }  // namespace tcg
 
-__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
-  hi = __float2bfloat16_rn(x);
-  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
-}
-__device__ __forceinline__ void put_pair(__nv_bfloat16 *hi, __nv_bfloat16 *lo, size_t pair,
-                                         float a, float b) {
-  __nv_bfloat16 h0, l0, h1, l1;
-  split_bf16(a, h0, l0);
-  split_bf16(b, h1, l1);
-  reinterpret_cast<__nv_bfloat162 *>(hi)[pair] = __halves2bfloat162(h0, h1);
-  reinterpret_cast<__nv_bfloat162 *>(lo)[pair] = __halves2bfloat162(l0, l1);
-}
 
 // B_y [Rp, Kp] from [H_r; H_d] [K, R] complex: 32 x 32 complex tiles turned
 // through shared memory (reads coalesced over r, writes over k); entries
@@ -1205,9 +1594,10 @@ __global__ void __launch_bounds__(128, 1)
 
 int round_up(long long v, int m) { return (int)((v + m - 1) / m * m); }
 
-// split of a k range of nkb blocks over enough CTAs for one wave
+// split of a k range of nkb blocks so that the CTAs fill about one wave
 void pick_split(int ntiles, int nkb, int sms, int &ks, int &kper) {
-  int want = std::max(1, (sms + ntiles - 1) / ntiles);
+  // one CTA fits an SM (shared memory), so keep tiles x splits within a wave
+  int want = std::max(1, sms / ntiles);
   want = std::min(want, nkb);
   kper = (nkb + want - 1) / want;
   ks = (nkb + kper - 1) / kper;
@@ -1226,7 +1616,7 @@ ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
   L.U = o; o += al(8 * (size_t)sp.kspl * C * R);          // Y partials
   L.G1 = o; o += al(8 * (size_t)C * R);
   L.G2 = o; o += al(8 * (size_t)C * R);
-  L.part = o; o += al(16 * (size_t)sp.nb_epi);
+  L.part = o; o += al(16 * (size_t)std::max(sp.nb_epi, (R + 31) / 32));  // either epilogue
   L.GU = o; o += al(8 * (size_t)sp.rspl * C * sp.K);      // G_U partials
   const int nsm = 512;                                    // CTA partials of the streaming path
   L.Pp = o; o += al(8 * (size_t)nsm * 2 * C * sp.K);
@@ -1278,7 +1668,7 @@ struct ObjTcPlan {
   CUtensorMap m_byh, m_byl, m_bgh, m_bgl, m_ayh, m_ayl, m_agh, m_agl;
   char *mem;      // one allocation: operands then scratch
   size_t bytes;
-  size_t oCtl, oU, oY, oG1, oG2, oPart, oGU, oGw;  // byte offsets in mem
+  size_t oCtl, oU, oY, oG1, oG2, oPart, oGU, oGUs, oDw;  // byte offsets in mem
 };
 
 cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr, int S, int M,
@@ -1311,9 +1701,10 @@ cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr
   p->oY = o; o += al(8 * (size_t)p->ksy * Cmax * R);
   p->oG1 = o; o += al(8 * (size_t)Cmax * R);
   p->oG2 = o; o += al(8 * (size_t)Cmax * R);
-  p->oPart = o; o += al(16 * (size_t)((R + 127) / 128));
+  p->oPart = o; o += al(16 * (size_t)((R + 31) / 32));
   p->oGU = o; o += al(8 * (size_t)p->ksg * Cmax * p->K);
-  p->oGw = o; o += al(8 * (size_t)((M + 31) / 32) * Cmax * S);
+  p->oGUs = o; o += al(8 * (size_t)Cmax * p->K);
+  p->oDw = o; o += al(8 * (size_t)Cmax * kDwParts * S);
   p->bytes = o;
   cudaError_t e = cudaMalloc(&p->mem, o);
   if (e != cudaSuccess) { delete p; return e; }
@@ -1375,7 +1766,6 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
   float *G2 = C > 1 ? reinterpret_cast<float *>(p->mem + p->oG2) : nullptr;
   double *part = reinterpret_cast<double *>(p->mem + p->oPart);
   float *GUp = reinterpret_cast<float *>(p->mem + p->oGU);
-  float *gw = reinterpret_cast<float *>(p->mem + p->oGw);
   float *scal = reinterpret_cast<float *>(ctl);
   unsigned *counter = reinterpret_cast<unsigned *>(ctl + 32);
   unsigned *err = reinterpret_cast<unsigned *>(ctl + 48);
@@ -1386,21 +1776,48 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
   dim3 gy(p->Rp / tcg::BN, p->Mp / tcg::BM, p->ksy);
   k_cgemm3<<<gy, 128, tcg::SMEM, st>>>(p->m_ayh, p->m_ayl, p->m_byh, p->m_byl, p->kpy,
                                         p->Kp / tcg::BK, C, R, R, Ypart, err);
-  k_epilogue<CB><<<(R + 127) / 128, 128, 0, st>>>(a, p->ksy, Ypart, G1, G2, part, counter, scal);
+  const bool need_g = a.grad_W || a.grad_phi;
+  if (CB >= 8) {
+    constexpr int CW = CB >= 8 ? CB : 8;
+    float *maxr = G1;  // G1 / G2 are not needed on this branch: per-Rx max and argmax
+    int *argr = reinterpret_cast<int *>(G2 ? G2 : G1 + R);
+    const int nb = (R + 31) / 32;
+    k_tc_epi_a<CW><<<nb, 256, 0, st>>>(a, p->ksy, Ypart, maxr, argr, part, counter, scal);
+    if (need_g || a.grad_Y) {
+      // with no gradient wanted the A operand is still written (harmless)
+      const int nbb = std::max(nb, (p->K2p / 2 + 31) / 32);
+      k_tc_epi_b<CW><<<nbb, 256, 0, st>>>(a, p->ksy, Ypart, maxr, argr, scal, p->K2p, p->ag_hi,
+                                          p->ag_lo);
+    }
+  } else {
+    k_epilogue<CB><<<(R + 127) / 128, 128, 0, st>>>(a, p->ksy, Ypart, G1, G2, part, counter,
+                                                    scal);
+    if (a.grad_Y) {
+      const long long n = (long long)C * R;
+      k_grad_y<<<(int)((n + 255) / 256), 256, 0, st>>>(G1, G2, scal, n, a.grad_Y);
+    }
+    if (need_g) {
+      const long long nag = (long long)C * (p->K2p / 2);
+      k_tc_make_ag<<<(unsigned)((nag + 255) / 256), 256, 0, st>>>(G1, G2, scal, C, R, p->K2p,
+                                                                  p->ag_hi, p->ag_lo);
+    }
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  if (a.grad_Y) {
-    const long long n = (long long)C * R;
-    k_grad_y<<<(int)((n + 255) / 256), 256, 0, st>>>(G1, G2, scal, n, a.grad_Y);
-  }
-  if (!a.grad_W && !a.grad_phi) return cudaGetLastError();
-  const long long nag = (long long)C * (p->K2p / 2);
-  k_tc_make_ag<<<(unsigned)((nag + 255) / 256), 256, 0, st>>>(G1, G2, scal, C, R, p->K2p,
-                                                              p->ag_hi, p->ag_lo);
+  if (!need_g) return cudaGetLastError();
   dim3 gg(p->Np / tcg::BN, p->Mp / tcg::BM, p->ksg);
   k_cgemm3<<<gg, 128, tcg::SMEM, st>>>(p->m_agh, p->m_agl, p->m_bgh, p->m_bgl, p->kpg,
                                         p->K2p / tcg::BK, C, p->K, p->K, GUp, err);
-  k_final<CB><<<(M + 31) / 32, 256, 0, st>>>(a, M, p->K, p->ksg, U, GUp, gw, counter + 1);
+  float *GU = reinterpret_cast<float *>(p->mem + p->oGUs);
+  const long long ngu = (long long)C * p->K;
+  k_gu_reduce<<<(unsigned)((ngu + 255) / 256), 256, 0, st>>>(GUp, p->ksg, ngu, GU);
+  if (a.grad_phi) k_tc_dphi<<<(M + 31) / 32, 256, 0, st>>>(GU, U, C, M, p->K, a.grad_phi);
+  if (a.grad_W) {
+    float *dwp = reinterpret_cast<float *>(p->mem + p->oDw);
+    k_tc_dw_part<<<dim3(C, kDwParts), 128, 0, st>>>(GU, p->Ha, a.phi, a.max_phase, p->S, M,
+                                                    p->K, dwp);
+    k_tc_dw_sum<<<(C * p->S + 127) / 128, 128, 0, st>>>(GU, dwp, C, p->S, M, p->K, a.grad_W);
+  }
   return cudaGetLastError();
 }
 }  // namespace

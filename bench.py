@@ -209,6 +209,111 @@ def objective_bench(torch, steps, flush):
             "gpu_launches_per_eval": 4}
 
 
+def objective_codes_bench(torch, R=4096, C=60, nset=4, reps=20):
+    """Codebook objective+grad (C codes, the reference Model's use) on the
+    tensor-core plan path (two tcgen05 3xBF16 GEMMs per evaluation) and on the
+    FP32 CUDA-core path, S=16, M=1024.  `nset` channel sets are evaluated in
+    turn so that the plan operands (about 8 (M+S) R bytes each way) exceed L2;
+    each evaluation is replayed from a CUDA graph."""
+    import ctypes as C_
+
+    from automs_gb300._lib import call, lib
+    L = lib()
+    rng = np.random.Generator(np.random.PCG64(2))
+    S, M = 16, 1024
+    lam = 3e8 / 60e9
+
+    def cn(*sh):
+        d = rng.uniform(2.0, 15.0, size=sh)
+        g = (rng.normal(size=sh) + 1j * rng.normal(size=sh)) / np.sqrt(2)
+        return torch.as_tensor((g * lam / (4 * np.pi * d)).astype(np.complex64), device="cuda")
+    P = lambda t: C_.c_void_p(t.data_ptr())
+    st = torch.cuda.Stream()
+    sets, plans = [], []
+    for _ in range(nset):
+        Hd, Ha, Hr = cn(S, R), cn(S, M), cn(M, R)
+        h = C_.c_void_p()
+        call("ams_objective_plan_create", P(Hd), P(Ha), P(Hr), S, M, R, C, C_.c_void_p(st.cuda_stream),
+             C_.byref(h))
+        sets.append((Hd, Ha, Hr))
+        plans.append(h)
+    phi = torch.as_tensor(rng.uniform(0, 2 * np.pi, M).astype(np.float32), device="cuda")
+    th = rng.uniform(0, 2 * np.pi, size=(C, S))
+    W = torch.as_tensor(np.exp(-1j * th).astype(np.complex64), device="cuda")
+    loss = torch.empty(nset, device="cuda")
+    gW = torch.empty(nset, C, S, dtype=torch.complex64, device="cuda")
+    gphi = torch.empty(nset, M, device="cuda")
+    z = C_.c_void_p(0)
+
+    def ev_tc():
+        for i, h in enumerate(plans):
+            call("ams_objective_plan_fwd_bwd", h, P(phi), float(2 * np.pi), P(W), C, 1.0 / R, z,
+                 P(loss[i]), P(gW[i]), P(gphi[i]), z, z, C_.c_void_p(st.cuda_stream))
+
+    def ev_cc():
+        for i, (Hd, Ha, Hr) in enumerate(sets):
+            call("ams_objective_fwd_bwd", P(Hd), P(Ha), P(Hr), P(phi), float(2 * np.pi), P(W), S,
+                 M, R, C, 1.0 / R, z, P(loss[i]), P(gW[i]), P(gphi[i]), z, z,
+                 C_.c_void_p(st.cuda_stream))
+
+    def timed(fn, n):
+        with torch.cuda.stream(st):
+            for _ in range(3):
+                fn()
+            st.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=st):
+                fn()
+            for _ in range(3):
+                g.replay()
+            st.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(n):
+                g.replay()
+            e1.record(st)
+            st.synchronize()
+        return e0.elapsed_time(e1) / (n * nset)
+    t_tc = timed(ev_tc, reps)
+    loss_tc = loss.clone()
+    t_cc = timed(ev_cc, max(2, reps // 4))
+    rel = float(((loss_tc - loss).abs() / loss.abs()).max())
+    K = M + S
+    Kp = -(-2 * K // 64) * 64
+    Rp = -(-R // 128) * 128
+    Np = -(-K // 128) * 128
+    K2p = -(-2 * R // 64) * 64
+    op_bytes = 4 * (Rp * Kp + Np * K2p)                 # B_y and B_g, hi + lo
+    mma_flop = 3 * 2 * 128 * (Kp * Rp + K2p * Np)        # executed on the tensor pipe
+    alg_flop = 16 * C * K * R                            # complex fwd + adjoint
+    hbm, kind = peaks()
+    bf16 = 1913.2
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            bf16 = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        pass
+    for h in plans:
+        L.ams_objective_plan_destroy(h)
+    gbs = op_bytes / (t_tc * 1e-3) / 1e9
+    tfl = mma_flop / (t_tc * 1e-3) / 1e12
+    return {"metric": f"objective+grad evals/s, {C}-code codebook", "value": 1e3 / t_tc,
+            "unit": "evals/s", "ms_per_eval": t_tc,
+            "config": {"S": S, "M": M, "R": R, "C": C,
+                       "l2": f"{nset} channel sets in turn ({nset * op_bytes / 1e6:.0f} MB of "
+                             "plan operands), CUDA-graph replay"},
+            "cuda_core_path": {"value": 1e3 / t_cc, "ms_per_eval": t_cc},
+            "speedup_vs_cuda_core": t_cc / t_tc,
+            "max_rel_loss_diff_vs_cuda_core": rel,
+            "algorithmic_tflops": alg_flop / (t_tc * 1e-3) / 1e12,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": gbs / hbm, "bytes_per_eval": op_bytes, "peak_kind": kind},
+            "roofline_tensor": {"bound": "tensor", "achieved": tfl, "peak": bf16,
+                                "unit": "TFLOP/s", "frac": tfl / bf16,
+                                "mma_flop_per_eval": mma_flop, "peak_kind": "measured bf16 burst"}}
+
+
 def channel_ms_bench(torch, warmup, steps, flush):
     """Channel set with one 32x32 metasurface on a 50k-triangle scene, 256x256
     Rx grid, 3 reflections, 1000x1000 launches: the AP->Rx, AP->MS and MS->Rx
@@ -310,8 +415,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="all", choices=["all", "tracer", "objective", "ms"],
+    ap.add_argument("--only", default="all",
+                    choices=["all", "tracer", "objective", "ms", "codes"],
                     help="profiling aid: run only the named timed loop")
+    ap.add_argument("--codes-r", type=int, default=0, choices=[0, 4096, 65536],
+                    help="profiling aid: run the codebook leg at one Rx count only")
     ap.add_argument("--launch", type=int, default=0,
                     help="profiling aid: override the forward launch edge (default 1000)")
     args = ap.parse_args()
@@ -338,6 +446,12 @@ def main():
         flushbuf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
         print(json.dumps(channel_ms_bench(torch, 1, max(1, args.steps),
                                           lambda: flushbuf.fill_(1.0))))
+        return
+    if args.only == "codes":
+        if args.codes_r in (0, 4096):
+            print(json.dumps(objective_codes_bench(torch, R=4096)))
+        if args.codes_r in (0, 65536):
+            print(json.dumps(objective_codes_bench(torch, R=65536, nset=1)))
         return
     if args.only == "objective":
         flushbuf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
