@@ -149,8 +149,13 @@ class Model(nn.Module):
     does (go.py:219-220); pass drop_rate=0 to disable it."""
 
     def __init__(self, name, channels, ms_list, max_ms_reflex=2, code_num=60, w=1.0,
-                 global_random=False, drop_rate=0.1, device="cuda"):
+                 global_random=False, drop_rate=0.1, device="cuda", tensor_cores="auto"):
         super().__init__()
+        # codebooks of 8 or more codes on one metasurface hop evaluate on the
+        # tensor-core plan path (ObjectivePlan, one per channel set)
+        self.tensor_cores = (code_num >= 8 and code_num <= 64) if tensor_cores == "auto" \
+            else bool(tensor_cores)
+        self._plans = {}
         if isinstance(channels, dict):
             channels = [channels]
         self.name = name
@@ -223,9 +228,16 @@ class Model(nn.Module):
             ch = self.pick_channel(True)
             use_ms = len(self.ms_list) == 1 and self.max_ms_reflex >= 1
             if use_ms:
+                plan = None
+                if self.tensor_cores:
+                    plan = self._plans.get(id(ch))
+                    if plan is None:
+                        plan = ObjectivePlan(ch["src_to_dst"], ch["src_to_ms{0}"],
+                                             ch["ms{0}_to_dst"], c_max=C_)
+                        self._plans[id(ch)] = plan
                 loss, recv = capacity_objective(
                     W, ch["src_to_dst"], ch["src_to_ms{0}"], ch["ms{0}_to_dst"], self.ms_theta[0],
-                    self.ms_list[0].max_phase, self.w, drop, return_recv=True)
+                    self.ms_list[0].max_phase, self.w, drop, return_recv=True, plan=plan)
             else:
                 loss, recv = capacity_objective(W, ch["src_to_dst"], w=self.w, drop=drop,
                                                 return_recv=True)

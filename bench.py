@@ -314,6 +314,52 @@ def objective_codes_bench(torch, R=4096, C=60, nset=4, reps=20):
                                 "mma_flop_per_eval": mma_flop, "peak_kind": "measured bf16 burst"}}
 
 
+def surrogate_bench(torch, n_train=400, n_pool=200, top_frac=0.05):
+    """Surrogate-screened placement search against the plain trace + adjoint
+    loop.  A placement study (12x8x3 m room, 12 boxes, 16-element AP, 128x128
+    Rx pooled 2x2 to a 64x64 gain map, metasurfaces of 8x8 to 24x24 on three
+    walls) traces n_train + n_pool placements; the MLP 72 -> 4x512 -> 4096
+    (BF16 tcgen05 GEMMs, FP32 master weights) is trained on the first set;
+    on the pool the surrogate ranks every placement and the tracer judges
+    the top top_frac.  configs/s: plain = 1 / t_trial, screened =
+    n_pool / (t_rank + judged * t_trial)."""
+    from automs_gb300 import placement, surrogate
+    t0 = time.perf_counter()
+    study = placement.PlacementStudy(seed=3, rx=(128, 128), launch=200, pool=2, opt_steps=12)
+    Xtr, Ytr, _ = study.dataset(n_train, seed=1)
+    t1 = time.perf_counter()
+    Xva, Yva, Pva = study.dataset(n_pool, seed=2)
+    t_trial = (time.perf_counter() - t1) / n_pool  # one plain trace + adjoint trial
+    t_data = time.perf_counter() - t0
+    mu, sd = Ytr.mean(0), Ytr.std() + 1e-6
+    net = surrogate.MLP([Xtr.shape[1], 512, 512, 512, 512, Ytr.shape[1]], max_batch=4096, seed=0)
+    t0 = time.perf_counter()
+    hist = net.fit(torch.as_tensor(Xtr).cuda(), torch.as_tensor((Ytr - mu) / sd).cuda(),
+                   epochs=150, batch=64, lr=1e-3, lr_decay=0.99)
+    torch.cuda.synchronize()
+    t_fit = time.perf_counter() - t0
+    mu_t = torch.as_tensor(mu, device="cuda")
+
+    def predict(X):
+        return net(X) * sd + mu_t
+    rep = placement.screening_report(study, predict, Pva, Yva, top_frac=top_frac,
+                                     t_trial=t_trial)
+    net.close()
+    return {"metric": "placement configs/s, surrogate-screened vs plain",
+            "value": rep["screened_configs_per_s"], "unit": "configs/s",
+            "plain_configs_per_s": rep["plain_configs_per_s"],
+            "ratio": rep["screened_configs_per_s"] / rep["plain_configs_per_s"],
+            "surrogate_median_abs_err_db": rep["surrogate_median_abs_err_db"],
+            "mean_predictor_median_abs_err_db": rep["mean_predictor_median_abs_err_db"],
+            "selection_gap_db": rep["selection_gap_db"],
+            "pick_median_cell_err_db": rep["pick_median_cell_err_db"],
+            "config": {"workload": "placement study: 128x128 Rx pooled to 64x64, MLP 72-4x512-4096",
+                       "train_samples": n_train, "pool": n_pool, "judged": rep["judged"],
+                       "t_trial_s": rep["t_trial_s"], "t_rank_s": rep["t_rank_s"],
+                       "t_dataset_s": t_data, "t_fit_s": t_fit,
+                       "fit_loss_first_last": [hist[0], hist[-1]]}}
+
+
 def channel_ms_bench(torch, warmup, steps, flush):
     """Channel set with one 32x32 metasurface on a 50k-triangle scene, 256x256
     Rx grid, 3 reflections, 1000x1000 launches: the AP->Rx, AP->MS and MS->Rx
@@ -415,8 +461,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="skip the codebook, channel-set and surrogate legs")
     ap.add_argument("--only", default="all",
-                    choices=["all", "tracer", "objective", "ms", "codes"],
+                    choices=["all", "tracer", "objective", "ms", "codes", "surrogate"],
                     help="profiling aid: run only the named timed loop")
     ap.add_argument("--codes-r", type=int, default=0, choices=[0, 4096, 65536],
                     help="profiling aid: run the codebook leg at one Rx count only")
@@ -446,6 +494,9 @@ def main():
         flushbuf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
         print(json.dumps(channel_ms_bench(torch, 1, max(1, args.steps),
                                           lambda: flushbuf.fill_(1.0))))
+        return
+    if args.only == "surrogate":
+        print(json.dumps(surrogate_bench(torch)))
         return
     if args.only == "codes":
         if args.codes_r in (0, 4096):
@@ -539,6 +590,12 @@ def main():
            "note": "Scene creation (copies + triangle BVH) + trace + result download per step"}
 
     obj = objective_bench(torch, 200, flush)
+    secondary = [obj]
+    if not args.no_secondary:
+        secondary.append(objective_codes_bench(torch, R=4096))
+        secondary.append(objective_codes_bench(torch, R=65536, nset=1))
+        secondary.append(channel_ms_bench(torch, 1, 1, flush))
+        secondary.append(surrogate_bench(torch))
 
     if rank != 0:
         if world > 1:
@@ -589,7 +646,7 @@ def main():
                          "peak_kind": "152 SM x 128 lanes x 2 at the sampled SM clock"},
         "cpu_baseline": cpu,
         "clocks": clocks,
-        "secondary": [obj],
+        "secondary": secondary,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
