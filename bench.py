@@ -58,10 +58,14 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi takes a moment to start: begin timing once it samples
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -97,6 +101,24 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def profile_value(name, key):
+    """A measured figure from a committed ncu summary under profiles/ (a line
+    'key: N'), or None."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.strip().startswith(key + ":"):
+                return int(line.split(":", 1)[1].strip())
+    return None
+
+
+def stage2_traffic():
+    """DRAM bytes (read + write) of k_stage2 over one coverage-128 trace."""
+    return profile_value("k_stage2_coverage128_traffic.md", "traffic_bytes_per_trace")
 
 
 def kernel_launches(stats, aabbs_given):
@@ -203,9 +225,12 @@ def objective_bench(torch, steps, flush):
             "ms_per_eval": t, "evals": reps * NSET,
             "config": {"S": S, "M": M, "R": R, "C": 1,
                        "l2": "8 channel sets (274 MB) evaluated in turn, CUDA-graph replay"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
-                         "algorithmic_bytes": bytes_alg, "peak_kind": kind},
+            "roofline": {"bound": "hbm", "kernel": "k_obj_stream", "achieved": achieved,
+                         "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": profile_value("k_obj_stream_c1_traffic.md",
+                                                  "traffic_bytes_per_launch"),
+                         "algorithmic_bytes": bytes_alg, "peak_kind": kind,
+                         "note": "achieved = algorithmic bytes / whole-evaluation time"},
             "gpu_launches_per_eval": 4}
 
 
@@ -307,8 +332,13 @@ def objective_codes_bench(torch, R=4096, C=60, nset=4, reps=20):
             "speedup_vs_cuda_core": t_cc / t_tc,
             "max_rel_loss_diff_vs_cuda_core": rel,
             "algorithmic_tflops": alg_flop / (t_tc * 1e-3) / 1e12,
-            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
-                         "frac": gbs / hbm, "bytes_per_eval": op_bytes, "peak_kind": kind},
+            "roofline": {"bound": "hbm", "kernel": "k_cgemm3 (both GEMMs)", "achieved": gbs,
+                         "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                         "bytes_per_eval": op_bytes, "peak_kind": kind,
+                         "traffic": profile_value("k_cgemm3_codebook60_r65536.md",
+                                                  "traffic_bytes_per_eval")
+                         if R == 65536 else None,
+                         "note": "achieved = plan operand bytes / whole-evaluation time"},
             "roofline_tensor": {"bound": "tensor", "achieved": tfl, "peak": bf16,
                                 "unit": "TFLOP/s", "frac": tfl / bf16,
                                 "mma_flop_per_eval": mma_flop, "peak_kind": "measured bf16 burst"}}
@@ -457,7 +487,7 @@ def channel_ms_bench(torch, warmup, steps, flush):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -611,11 +641,7 @@ def main():
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
     flops = FLOP_PER_SEGMENT * st0["segments_bwd"]
     tflops = flops / (k2_ms * 1e-3) / 1e12 if k2_ms > 0 else 0.0
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            traffic = json.load(f).get("k_stage2_bytes_per_launch_coverage128")
+    traffic = stage2_traffic()
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
