@@ -209,9 +209,9 @@ __device__ __forceinline__ bool prim_slab(const RayT &r, float4 lo, float4 hi) {
 }
 
 // __intersection__sphere, optixPathTracer.cu:419-445; t = closest approach
-__device__ __forceinline__ float sphere_hit(const RayT &r, af3 center, float radius) {
+// D = d * (1 / |d|) is passed in: the same for every sphere of one query
+__device__ __forceinline__ float sphere_hit(const RayT &r, af3 D, af3 center, float radius) {
   af3 O = sub3(center, r.o);
-  af3 D = scl3(r.d, 1.0f / len3(r.d));
   float b = dot3(O, D);
   float c = dot3(O, O);
   float acc = fmaxf(5e-5f, radius * radius);
@@ -244,9 +244,13 @@ __device__ __forceinline__ bool child_test(const RayT &r, float lx, float ly, fl
          tn <= __fmaf_rn(best, 1.0001f, 1e-4f);
 }
 
+__device__ __forceinline__ af3 unit_dir(const RayT &r) { return scl3(r.d, 1.0f / len3(r.d)); }
+
+// INST 2 (the many Rx spheres) uses the unit direction computed once per
+// query; INST 1 (Tx spheres, rarely past the slab gate) computes it here
 template <int INST>
 __device__ __forceinline__ void test_prim(const float4 *prims, int j, const RayT &r, Hit &best,
-                                          float radius) {
+                                          float radius, const af3 &Dq) {
   const float4 a = __ldg(prims + 3 * j);
   const float4 b = __ldg(prims + 3 * j + 1);
   const float4 c = __ldg(prims + 3 * j + 2);
@@ -258,7 +262,7 @@ __device__ __forceinline__ void test_prim(const float4 *prims, int j, const RayT
     }
   } else {
     if (!prim_slab(r, b, c)) return;
-    float t = sphere_hit(r, mk3(a.x, a.y, a.z), radius);
+    float t = sphere_hit(r, INST == 2 ? Dq : unit_dir(r), mk3(a.x, a.y, a.z), radius);
     if (t >= 0.0f && better(t, INST, orig, best)) {
       best.t = t; best.inst = INST; best.prim = orig;
     }
@@ -272,7 +276,9 @@ template <int INST>
 __device__ void traverse(const BvhNode *nodes, const float4 *prims, int n, const RayT &r,
                          Hit &best, float radius, unsigned *err) {
   if (n <= 0) return;
-  if (n == 1) { test_prim<INST>(prims, 0, r, best, radius); return; }
+  af3 Dq = mk3(0.f, 0.f, 0.f);
+  if (INST == 2) Dq = unit_dir(r);
+  if (n == 1) { test_prim<INST>(prims, 0, r, best, radius, Dq); return; }
   int st_node[AMS_STACK];
   float st_t[AMS_STACK];
   int sp = 0;
@@ -287,12 +293,12 @@ __device__ void traverse(const BvhNode *nodes, const float4 *prims, int n, const
     bool h1 = child_test(r, b.z, b.w, c.x, c.y, c.z, c.w, best.t, tn1);
     if (h0 && d.x < 0) {
       if (~d.x >= n) { atomicOr(err, AMS_DERR_BVH); return; }
-      test_prim<INST>(prims, ~d.x, r, best, radius);
+      test_prim<INST>(prims, ~d.x, r, best, radius, Dq);
       h0 = false;
     }
     if (h1 && d.y < 0) {
       if (~d.y >= n) { atomicOr(err, AMS_DERR_BVH); return; }
-      test_prim<INST>(prims, ~d.y, r, best, radius);
+      test_prim<INST>(prims, ~d.y, r, best, radius, Dq);
       h1 = false;
     }
     if (h0 && h1) {
@@ -327,9 +333,14 @@ __device__ __forceinline__ Hit closest(const TraceDev &P, af3 o, af3 d, int mask
   ray_setup(r, o, d);
   Hit h;
   h.t = AMS_TMAX; h.inst = 3; h.prim = 0x7fffffff;
+  // The result is the lexicographic minimum of (t, instance, primitive) over
+  // all primitives, so the order of the traversals changes nothing but the
+  // work: Rx spheres first (most forward segments end a few cm ahead on one),
+  // then the scene pruned at that distance.  (A per-segment choice of order
+  // measured slower: two inlined copies of the sphere traversal.)
+  if (mask & 4) traverse<2>(P.rx_nodes, P.rx_prims, P.n_dst, r, h, P.dst_r, P.err);
   if (mask & 1) traverse<0>(P.tri_nodes, P.tri_prims, P.n_tri, r, h, 0.0f, P.err);
   if (mask & 2) traverse<1>(P.tx_nodes, P.tx_prims, P.n_src, r, h, P.src_r, P.err);
-  if (mask & 4) traverse<2>(P.rx_nodes, P.rx_prims, P.n_dst, r, h, P.dst_r, P.err);
   return h;
 }
 
@@ -390,12 +401,20 @@ __device__ __forceinline__ uint32_t key_hash32(const int32_t *k) {
 }
 
 // claim or find the slot of a path key; returns -1 when the table is full
+// OR a bit into a bitmap word unless it is already set (skips the atomic
+// for the many records of a (cell, path) pair that is already marked)
+__device__ __forceinline__ void set_bit(unsigned *word, unsigned bit) {
+  if (!(__ldcg(word) & bit)) atomicOr(word, bit);
+}
+
 __device__ int path_insert(const TraceDev &P, const int32_t *key) {
   const uint64_t h = key_hash64(key) | 1ull;
   const uint32_t c = key_hash32(key) | 1u;
   uint32_t slot = (uint32_t)h & P.tab_mask;
   for (uint32_t probe = 0; probe <= P.tab_mask; probe++) {
-    unsigned long long old = atomicCAS(P.tab_h + slot, 0ull, (unsigned long long)h);
+    // most records repeat a key already in the table: look before the CAS
+    unsigned long long old = __ldcg(P.tab_h + slot);
+    if (old == 0ull) old = atomicCAS(P.tab_h + slot, 0ull, (unsigned long long)h);
     if (old == 0ull) {
       int32_t *dst = P.tab_key + (size_t)slot * 14;
 #pragma unroll
@@ -407,7 +426,8 @@ __device__ int path_insert(const TraceDev &P, const int32_t *key) {
       return (int)slot;
     }
     if (old == (unsigned long long)h) {
-      unsigned o = atomicCAS(P.tab_chk + slot, 0u, c);
+      unsigned o = __ldcg(P.tab_chk + slot);
+      if (o == 0u) o = atomicCAS(P.tab_chk + slot, 0u, c);
       if (o != 0u && o != c) atomicOr(P.err, AMS_DERR_HASH);
       return (int)slot;
     }
@@ -508,7 +528,7 @@ __global__ void __launch_bounds__(128, 7) k_stage1(TraceDev P) {
                 key[13] = i;
                 int slot = path_insert(P, key);
                 if (slot >= 0)
-                  atomicOr(P.T + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
+                  set_bit(P.T + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
                 my_records++;
               }
             } else {
