@@ -617,6 +617,10 @@ ams_status ams_objective_plan_fwd_bwd(ams_objective_plan *plan, const float *phi
     return AMS_ERR_ARG;
   }
   if (!(max_phase > 0.f)) { set_err(errbuf, errlen, "max_phase must be > 0"); return AMS_ERR_ARG; }
+  if (grad_Y && obj_tc_plan_streams(plan->p)) {
+    set_err(errbuf, errlen, "grad_Y is not available from a plan made with C_max <= 2");
+    return AMS_ERR_ARG;
+  }
   ObjArgs a{nullptr, nullptr, nullptr, phi, W, max_phase, plan->S, plan->M, plan->R, C, w, drop,
             loss, grad_W, grad_phi, recv_amp, grad_Y};
   CK(obj_tc_run(plan->p, a, (cudaStream_t)stream));

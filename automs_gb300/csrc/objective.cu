@@ -1382,6 +1382,215 @@ cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, 
 }
 
 // ------------------------------------------------------------------
+// Streaming path on a plan's transposed copy HT [Rp][Kp] of [H_r; H_d]
+// (row r = column r over all k): a tile of TR Rx is one contiguous block of
+// TR * Kp * 8 bytes, fetched by a single cp.async.bulk instead of one 32-byte
+// piece per row.  Phases as in k_obj_stream; in (A) warp w takes column
+// w % TR and every (NW / TR)-th run of 32 k, lanes over k.
+
+__global__ void __launch_bounds__(256) k_make_ht(const float *Hr, const float *Hd, int M, int S,
+                                                 int R, int Rp, int Kp, float *HT) {
+  __shared__ float2 tl[32][33];
+  const int r0 = blockIdx.x * 32, k0 = blockIdx.y * 32, K = M + S;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int k = k0 + i, r = r0 + threadIdx.x;
+    float2 v = make_float2(0.f, 0.f);
+    if (k < K && r < R)
+      v = __ldg(reinterpret_cast<const float2 *>(k < M ? Hr + (size_t)k * R * 2
+                                                        : Hd + (size_t)(k - M) * R * 2) + r);
+    tl[i][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int r = r0 + i, k = k0 + threadIdx.x;
+    if (r < Rp && k < Kp) reinterpret_cast<float2 *>(HT)[(size_t)r * Kp + k] = tl[threadIdx.x][i];
+  }
+}
+
+template <int CB, int TR, int KPT>
+__global__ void __launch_bounds__(256)
+    k_obj_stream_t(ObjArgs a, const float *HT, int M, int Kp, int stage_bytes, int ntiles,
+                   const float *U, float *Ppart, double *lpart, unsigned *err) {
+  constexpr int NTH = 256, NW = NTH / 32, NPART = NW / TR;
+  const int K = M + a.S;
+  const uint32_t tile_bytes = (uint32_t)TR * Kp * 8;
+  extern __shared__ unsigned char smem_dyn[];
+  unsigned char *base = reinterpret_cast<unsigned char *>(
+      (reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
+  c2 *coef = reinterpret_cast<c2 *>(base + 2 * (size_t)stage_bytes);  // [K][CB]
+  __shared__ c2 red[NW][CB];
+  __shared__ c2 g1s[CB][TR], g2s[CB][TR];
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ int abort_flag;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+
+  auto issue = [&](int tile, int stage) {
+    uint64_t *bar = &full[stage];
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(tile_bytes)
+                 : "memory");
+    const float *src = HT + (size_t)tile * TR * Kp * 2;
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_addr(base + (size_t)stage * stage_bytes)),
+        "l"(reinterpret_cast<uint64_t>(src)), "r"(tile_bytes), "r"(smem_addr(bar))
+        : "memory");
+  };
+  const int first = blockIdx.x;
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[0])), "r"(1));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[1])), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+    if (first < ntiles) issue(first, 0);
+    if (first + (int)gridDim.x < ntiles) issue(first + gridDim.x, 1);
+  }
+  cudaGridDependencySynchronize();
+  for (int i = t; i < K * CB; i += NTH) {
+    const int k = i / CB, c = i % CB;
+    c2 v = {0.f, 0.f};
+    if (c < a.C) v = k < M ? ld2(U, (size_t)c * M + k) : ld2(a.W, (size_t)c * a.S + (k - M));
+    coef[i] = v;
+  }
+  __syncthreads();
+
+  c2 p1[KPT][CB], p2[KPT][CB];
+#pragma unroll
+  for (int q = 0; q < KPT; q++)
+#pragma unroll
+    for (int c = 0; c < CB; c++) { p1[q][c] = {0.f, 0.f}; p2[q][c] = {0.f, 0.f}; }
+  float sum_max = 0.f, sum_sq = 0.f;  // FP32 within a warp, FP64 across warps
+  const int acol = warp % TR, apart = warp / TR;
+
+  int it = 0;
+  for (int tile = first; tile < ntiles; tile += gridDim.x, it++) {
+    const int stg = it & 1;
+    if (!mbar_wait_bounded(&full[stg], (it >> 1) & 1)) {
+      if (t == 0) atomicOr(err, 1u);
+      abort_flag = 1;
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    const float2 *T = reinterpret_cast<const float2 *>(base + (size_t)stg * stage_bytes);
+    // (A) Y of column acol over this warp's runs of k
+    {
+      c2 y[CB];
+#pragma unroll
+      for (int c = 0; c < CB; c++) y[c] = {0.f, 0.f};
+      const float2 *row = T + (size_t)acol * Kp;
+#pragma unroll 4
+      for (int k = apart * 32 + lane; k < K; k += NPART * 32) {
+        const float2 h = row[k];
+#pragma unroll
+        for (int c = 0; c < CB; c++) mac(y[c], coef[(size_t)k * CB + c], c2{h.x, h.y});
+      }
+#pragma unroll
+      for (int c = 0; c < CB; c++)
+        for (int o = 16; o > 0; o >>= 1) {
+          y[c].x += __shfl_xor_sync(0xffffffffu, y[c].x, o);
+          y[c].y += __shfl_xor_sync(0xffffffffu, y[c].y, o);
+        }
+      if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < CB; c++) red[warp][c] = y[c];
+    }
+    __syncthreads();
+    // (B) per-Rx capacity, max, mask, gradient parts
+    if (t < TR) {
+      const int r = tile * TR + t;
+      c2 yy[CB];
+      float cap[CB], amp[CB];
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        c2 acc = {0.f, 0.f};
+#pragma unroll
+        for (int pp = 0; pp < NPART; pp++) {
+          acc.x += red[pp * TR + t][c].x;
+          acc.y += red[pp * TR + t][c].y;
+        }
+        yy[c] = acc;
+      }
+      int arg = 0;
+      float mx = -1.f;
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        if (c >= a.C) { cap[c] = 0.f; amp[c] = 0.f; continue; }
+        amp[c] = sqrtf(yy[c].x * yy[c].x + yy[c].y * yy[c].y);
+        const float aa = amp[c] + kEps;
+        float v = log2f(1.0f + aa * aa / kN0);
+        if (a.drop && a.drop[c]) v = 0.f;
+        cap[c] = v;
+        if (v > mx) { mx = v; arg = c; }
+        if (a.recv_amp && r < a.R) a.recv_amp[(size_t)c * a.R + r] = amp[c];
+      }
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        c2 ga = {0.f, 0.f}, gb = {0.f, 0.f};
+        if (c < a.C && r < a.R) {
+          const bool dropped = a.drop && a.drop[c];
+          const float msk = (cap[c] != mx) ? cap[c] : 0.f;
+          sum_sq += msk * msk;
+          const float aa = amp[c] + kEps;
+          const float dcap = (2.0f * aa / kN0) / (1.0f + aa * aa / kN0) * kInvLn2;
+          float g1 = (c == arg) ? -a.w : 0.f, g2 = msk;
+          if (dropped) { g1 = 0.f; g2 = 0.f; }
+          const float sc = amp[c] > 0.f ? dcap / amp[c] : 0.f;
+          ga = {g1 * sc * yy[c].x, g1 * sc * yy[c].y};
+          gb = {g2 * sc * yy[c].x, g2 * sc * yy[c].y};
+        }
+        g1s[c][t] = ga;
+        g2s[c][t] = gb;
+      }
+      if (r < a.R) sum_max += mx;
+    }
+    __syncthreads();
+    // (C) P += G conj(H) over the tile's columns, rows k = t + NTH q
+#pragma unroll
+    for (int q = 0; q < KPT; q++) {
+      const int k = t + NTH * q;
+      if (k < K) {
+#pragma unroll
+        for (int cc = 0; cc < TR; cc++) {
+          const float2 h = T[(size_t)cc * Kp + k];
+#pragma unroll
+          for (int c = 0; c < CB; c++) {
+            macc(p1[q][c], g1s[c][cc], c2{h.x, h.y});
+            if (CB > 1) macc(p2[q][c], g2s[c][cc], c2{h.x, h.y});
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (t == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (tile + 2 * (int)gridDim.x < ntiles) issue(tile + 2 * gridDim.x, stg);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < KPT; q++) {
+    const int k = t + NTH * q;
+    if (k >= K) continue;
+#pragma unroll
+    for (int c = 0; c < CB; c++) {
+      if (c >= a.C) continue;
+      float2 *o = reinterpret_cast<float2 *>(Ppart) + ((size_t)blockIdx.x * 2 * a.C + c) * K + k;
+      o[0] = make_float2(p1[q][c].x, p1[q][c].y);
+      if (CB > 1) o[(size_t)a.C * K] = make_float2(p2[q][c].x, p2[q][c].y);
+    }
+  }
+  if (t < 32) {
+    for (int o = 16; o > 0; o >>= 1) {
+      sum_max += __shfl_xor_sync(0xffffffffu, sum_max, o);
+      sum_sq += __shfl_xor_sync(0xffffffffu, sum_sq, o);
+    }
+    if (t == 0) {
+      lpart[2 * blockIdx.x] = sum_max;
+      lpart[2 * blockIdx.x + 1] = sum_sq;
+    }
+  }
+}
+
+// ------------------------------------------------------------------
 // Tensor-core path (tcgen05, 3xBF16 split precision, FP32 accumulation).
 //
 // A complex product over k becomes one real GEMM on interleaved real views;
@@ -1662,6 +1871,11 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
 // ------------------------------------------------------------------ plans
 struct ObjTcPlan {
   const float *Hd, *Ha, *Hr;
+  // stream mode (C_max <= 2): transposed FP32 copy and the streaming kernels
+  bool stream = false;
+  float *HT = nullptr;
+  int tKp = 0, tTR = 0, tKPT = 0, tStage = 0, tTiles = 0, tGrid = 0;
+  size_t tSmem = 0, oPp = 0, oLp = 0, oGwS = 0;
   int S, M, R, Cmax, K, Kp, Rp, Np, K2p, Mp;
   int ksy, kpy, ksg, kpg;
   __nv_bfloat16 *by_hi, *by_lo, *bg_hi, *bg_lo, *ay_hi, *ay_lo, *ag_hi, *ag_lo;
@@ -1670,6 +1884,119 @@ struct ObjTcPlan {
   size_t bytes;
   size_t oCtl, oU, oY, oG1, oG2, oPart, oGU, oGUs, oDw;  // byte offsets in mem
 };
+
+namespace {
+// Stream mode: HT [Rp][Kp] holds [H_r; H_d] transposed (FP32 complex, rows
+// padded to an even length so a tile is a whole number of 16-byte units).
+cudaError_t plan_stream_create(ObjTcPlan *p, cudaStream_t st, ObjTcPlan **out) {
+  const int K = p->K, CB = cbucket(p->Cmax), S = p->S, M = p->M, R = p->R;
+  const int kpt = (K + 255) / 256;
+  p->tKPT = kpt <= 4 ? 4 : (kpt <= 8 ? 8 : (kpt <= 16 ? 16 : 0));
+  if (!p->tKPT || (CB == 2 && p->tKPT > 8)) { delete p; return cudaErrorInvalidValue; }
+  p->tKp = (K + 1) / 2 * 2;
+  int per_sm = 2;
+  for (int TR : {8, 4, 2}) {
+    const size_t stage = ((size_t)TR * p->tKp * 8 + 1023) / 1024 * 1024;
+    const size_t smem = 1024 + 2 * stage + (size_t)K * CB * 8;
+    if (smem <= 110 * 1024) { p->tTR = TR; p->tStage = (int)stage; p->tSmem = smem; break; }
+  }
+  if (!p->tTR) {  // long columns: two-Rx tiles, one CTA per SM
+    const size_t stage = ((size_t)2 * p->tKp * 8 + 1023) / 1024 * 1024;
+    const size_t smem = 1024 + 2 * stage + (size_t)K * CB * 8;
+    if (smem > 220 * 1024) { delete p; return cudaErrorInvalidValue; }
+    p->tTR = 2; p->tStage = (int)stage; p->tSmem = smem;
+    per_sm = 1;
+  }
+  const int Rp = (R + p->tTR - 1) / p->tTR * p->tTR;
+  p->tTiles = Rp / p->tTR;
+  p->tGrid = std::min(per_sm * sm_count(), p->tTiles);
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  size_t o = 0;
+  const size_t oht = o; o += al(8 * (size_t)Rp * p->tKp);
+  p->oCtl = o; o += kObjControlBytes;
+  p->oU = o; o += al(8 * (size_t)p->Cmax * M);
+  p->oPp = o; o += al(8 * (size_t)p->tGrid * 2 * p->Cmax * K);
+  p->oLp = o; o += al(16 * (size_t)p->tGrid);
+  p->oGwS = o; o += al(8 * (size_t)((K + 7) / 8) * p->Cmax * S);
+  p->bytes = o;
+  cudaError_t e = cudaMalloc(&p->mem, o);
+  if (e != cudaSuccess) { delete p; return e; }
+  p->HT = reinterpret_cast<float *>(p->mem + oht);
+  p->stream = true;
+  e = cudaMemsetAsync(p->mem + p->oCtl, 0, kObjControlBytes, st);
+  if (e == cudaSuccess) {
+    dim3 g((Rp + 31) / 32, (p->tKp + 31) / 32), b(32, 8);
+    k_make_ht<<<g, b, 0, st>>>(p->Hr, p->Hd, M, S, R, Rp, p->tKp, p->HT);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) { cudaFree(p->mem); delete p; return e; }
+  *out = p;
+  return cudaSuccess;
+}
+
+template <int CB, int TR, int KPT>
+cudaError_t launch_stream_ht(ObjTcPlan *p, const ObjArgs &a, const float *U, float *Pp,
+                             double *lp, unsigned *err, cudaStream_t st) {
+  auto kfn = k_obj_stream_t<CB, TR, KPT>;
+  static size_t set_bytes = 0;
+  if (set_bytes < p->tSmem) {
+    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)p->tSmem);
+    if (e != cudaSuccess) return e;
+    set_bytes = p->tSmem;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(p->tGrid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = p->tSmem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kfn, a, (const float *)p->HT, p->M, p->tKp, p->tStage,
+                            p->tTiles, U, Pp, lp, err);
+}
+
+template <int CB, int TR>
+cudaError_t launch_stream_ht_k(ObjTcPlan *p, const ObjArgs &a, const float *U, float *Pp,
+                               double *lp, unsigned *err, cudaStream_t st) {
+  switch (p->tKPT) {
+    case 4: return launch_stream_ht<CB, TR, 4>(p, a, U, Pp, lp, err, st);
+    case 8: return launch_stream_ht<CB, TR, 8>(p, a, U, Pp, lp, err, st);
+    case 16:
+      if (CB == 1) return launch_stream_ht<1, TR, 16>(p, a, U, Pp, lp, err, st);
+      return cudaErrorInvalidValue;
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int CB>
+cudaError_t run_plan_stream(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st) {
+  const int M = p->M;
+  float *U = reinterpret_cast<float *>(p->mem + p->oU);
+  float *Pp = reinterpret_cast<float *>(p->mem + p->oPp);
+  double *lp = reinterpret_cast<double *>(p->mem + p->oLp);
+  float *gw = reinterpret_cast<float *>(p->mem + p->oGwS);
+  char *ctl = p->mem + p->oCtl;
+  unsigned *counter = reinterpret_cast<unsigned *>(ctl + 36);
+  unsigned *err = reinterpret_cast<unsigned *>(ctl + 48);
+  const long long n = (long long)M * a.C * 8;
+  k_prep_wide<<<(int)((n + 255) / 256), 256, 0, st>>>(a, M, U);
+  cudaError_t e;
+  switch (p->tTR) {
+    case 8: e = launch_stream_ht_k<CB, 8>(p, a, U, Pp, lp, err, st); break;
+    case 4: e = launch_stream_ht_k<CB, 4>(p, a, U, Pp, lp, err, st); break;
+    default: e = launch_stream_ht_k<CB, 2>(p, a, U, Pp, lp, err, st); break;
+  }
+  if (e != cudaSuccess) return e;
+  const int nbf = (M + a.S + 7) / 8;
+  k_stream_final<CB><<<nbf, 256, sizeof(float2) * a.C * a.S, st>>>(a, M, p->tGrid, Pp, lp, gw,
+                                                                     counter);
+  return cudaGetLastError();
+}
+}  // namespace
 
 cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr, int S, int M,
                                int R, int Cmax, cudaStream_t st, ObjTcPlan **out) {
@@ -1685,6 +2012,7 @@ cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr
   p->K2p = round_up(2LL * R, 64);
   p->Mp = round_up(2LL * Cmax, tcg::BM);
   const int sms = sm_count();
+  if (Cmax <= 2) return plan_stream_create(p, st, out);
   pick_split((p->Rp / tcg::BN) * (p->Mp / tcg::BM), p->Kp / tcg::BK, sms, p->ksy, p->kpy);
   pick_split((p->Np / tcg::BN) * (p->Mp / tcg::BM), p->K2p / tcg::BK, sms, p->ksg, p->kpg);
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -1749,6 +2077,7 @@ cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr
 }
 
 size_t obj_tc_plan_bytes(const ObjTcPlan *p) { return p ? p->bytes : 0; }
+bool obj_tc_plan_streams(const ObjTcPlan *p) { return p && p->stream; }
 
 void obj_tc_plan_destroy(ObjTcPlan *p) {
   if (!p) return;
@@ -1827,6 +2156,10 @@ cudaError_t obj_tc_run(ObjTcPlan *p, const ObjArgs &a0, cudaStream_t st) {
   ObjArgs a = a0;
   a.Hd = p->Hd; a.Ha = p->Ha; a.Hr = p->Hr;
   a.S = p->S; a.M = p->M; a.R = p->R;
+  if (p->stream) {
+    if (a.grad_Y) return cudaErrorInvalidValue;  // not produced by the streaming kernels
+    return cbucket(a.C) == 1 ? run_plan_stream<1>(p, a, st) : run_plan_stream<2>(p, a, st);
+  }
   char *ctl = p->mem + p->oCtl;
   switch (cbucket(a.C)) {
 #define CASE(CB) case CB: return run_tc<CB>(p, a, ctl, st);

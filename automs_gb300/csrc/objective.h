@@ -34,14 +34,17 @@ cudaError_t coverage_db_run(const float *H, int S, int R, float threshold, float
 // on a device looks up the array's device address
 cudaError_t obj_noalloc_scratch(char **out);
 
-// Tensor-core evaluation (tcgen05, 3xBF16 split precision) for a fixed
-// channel set with a metasurface hop: the plan holds BF16 hi/lo copies of
-// [H_r; H_d] in the two layouts the forward and adjoint GEMMs read, plus its
-// own scratch.  H_d, H_a and H_r must stay valid while the plan is used;
+// Evaluation plan for a fixed channel set with a metasurface hop.  Cmax > 2:
+// tensor cores (tcgen05, 3xBF16 split precision); the plan holds BF16 hi/lo
+// copies of [H_r; H_d] in the two layouts the forward and adjoint GEMMs read.
+// Cmax <= 2: streaming kernels over a transposed FP32 copy [R][M+S] (one
+// contiguous block per tile of Rx; grad_Y is not produced).  The plan owns
+// its scratch.  H_d, H_a and H_r must stay valid while the plan is used;
 // evaluations on one plan must not overlap.  1 <= C <= Cmax <= 64.
 struct ObjTcPlan;
 cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr, int S, int M,
                                int R, int Cmax, cudaStream_t st, ObjTcPlan **out);
 cudaError_t obj_tc_run(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st);
 size_t obj_tc_plan_bytes(const ObjTcPlan *p);
+bool obj_tc_plan_streams(const ObjTcPlan *p);
 void obj_tc_plan_destroy(ObjTcPlan *p);

@@ -167,19 +167,22 @@ ams_status ams_objective_fwd_bwd_noalloc(
     float *grad_Y, float *recv_amp, void *stream, char *errbuf, size_t errlen);
 
 /* Received amplitude |Y| [C,R] of the same model (forward only). */
-/* Tensor-core evaluation of ams_objective_fwd_bwd for a fixed channel set
- * (one metasurface hop), for codebooks (C up to 64) evaluated many times --
- * the optimizer loop of optimize_model (go.py:296-336) with the reference's
- * code_num.  No single counterpart in the reference: it replaces the
+/* Evaluation plan of ams_objective_fwd_bwd for a fixed channel set (one
+ * metasurface hop) evaluated many times -- the optimizer loop of
+ * optimize_model (go.py:296-336), with the reference's code_num codes or
+ * with C = 1.  No single counterpart in the reference: it replaces the
  * autograd forward/backward of Model.forward (go.py:159-245) when the
- * channels are fixed.  The plan converts [H_r; H_d] once into BF16 hi/lo
+ * channels are fixed.  With C_max > 2 it is the tensor-core path.  The plan converts [H_r; H_d] once into BF16 hi/lo
  * pairs (x = hi + lo, 3xBF16 products with FP32 accumulation, relative
  * error about 1e-5) in the two layouts of the forward and adjoint GEMMs
  * (tcgen05 tensor cores).  H_d, H_a, H_r must stay valid and unchanged while
  * the plan lives.  ams_objective_plan_fwd_bwd has the arguments and results
  * of ams_objective_fwd_bwd (the channels come from the plan); calls on one
  * plan must not overlap.  The plan owns about 8 (R (M+S) + (M+S) R) bytes of
- * device memory (ams_objective_plan_bytes). */
+ * device memory (ams_objective_plan_bytes).  A plan made with C_max <= 2
+ * instead holds one FP32 copy of [H_r; H_d] transposed to [R][M+S] and runs
+ * the single-pass streaming kernels over it (each tile of Rx is one
+ * contiguous block); it does not produce grad_Y (AMS_ERR_ARG). */
 typedef struct ams_objective_plan ams_objective_plan;
 ams_status ams_objective_plan_create(const float *H_d, const float *H_a,
                                      const float *H_r, int S, int M, int R,

@@ -184,6 +184,37 @@ def test_tensor_core_plan_vs_oracle(obj, name):
     plan.close()
 
 
+@pytest.mark.parametrize("name,c_max", [("c1", 1), ("cfg1_c1", 1), ("cfg1_c2", 2)])
+def test_streaming_plan_vs_oracle(obj, name, c_max):
+    """Plans made with C_max <= 2 stream a transposed FP32 copy of the
+    channels (one contiguous block per tile): same tolerances as the direct
+    path against the FP64 oracle."""
+    if name == "c1":
+        c = cases.objective_case("c1")
+    else:
+        c = _cfg1_codes(C=c_max, seed=9)
+    ch, theta_np, A, drop, mp = _tc_inputs(c)
+    Hd, Ha, Hr = ch["src_to_dst"], ch["src_to_ms{0}"], ch["ms{0}_to_dst"]
+    phi = c["phi"][0]
+    loss_o, gth_o, gphi_o, ex = OO.objective(Hd, Ha, Hr, phi, theta_np, A, c["w"], drop, mp)
+    plan = obj.ObjectivePlan(cuda(Hd), cuda(Ha), cuda(Hr), c_max=c_max)
+    theta = cuda(theta_np).requires_grad_(True)
+    W = cuda(A.astype(np.float32)) * torch.exp(-1j * theta)
+    ph = cuda(phi).requires_grad_(True)
+    for _ in range(2):  # a second call reuses the plan's scratch and counters
+        loss, recv = obj.capacity_objective(W, cuda(Hd), cuda(Ha), cuda(Hr), ph, mp, c["w"],
+                                            cuda(drop), return_recv=True, plan=plan)
+    loss.backward()
+    np.testing.assert_allclose(float(loss), loss_o, rtol=1e-4)
+    np.testing.assert_allclose(recv.cpu().numpy(), ex["amp"], rtol=1e-4,
+                               atol=1e-4 * np.abs(ex["amp"]).max())
+    g = theta.grad.cpu().numpy()
+    np.testing.assert_allclose(g, gth_o, rtol=1e-3, atol=1e-3 * np.abs(gth_o).max())
+    gp = ph.grad.cpu().numpy()
+    np.testing.assert_allclose(gp, gphi_o, rtol=1e-3, atol=1e-3 * np.abs(gphi_o).max())
+    plan.close()
+
+
 def test_tensor_core_plan_matches_cuda_core_path(obj):
     """Same evaluation on the plan and on the FP32 CUDA-core path, the plan
     reused across calls with different C, phi and dropout."""
