@@ -149,12 +149,12 @@ class Model(nn.Module):
     does (go.py:219-220); pass drop_rate=0 to disable it."""
 
     def __init__(self, name, channels, ms_list, max_ms_reflex=2, code_num=60, w=1.0,
-                 global_random=False, drop_rate=0.1, device="cuda", tensor_cores="auto"):
+                 global_random=False, drop_rate=0.1, device="cuda", plans=True):
         super().__init__()
-        # codebooks of 8 or more codes on one metasurface hop evaluate on the
-        # tensor-core plan path (ObjectivePlan, one per channel set)
-        self.tensor_cores = (code_num >= 8 and code_num <= 64) if tensor_cores == "auto" \
-            else bool(tensor_cores)
+        # one metasurface hop: an ObjectivePlan per channel set (made on first
+        # use; C <= 2 streams a transposed copy, larger codebooks run on the
+        # tensor cores)
+        self.use_plans = bool(plans) and code_num <= 64
         self._plans = {}
         if isinstance(channels, dict):
             channels = [channels]
@@ -229,7 +229,7 @@ class Model(nn.Module):
             use_ms = len(self.ms_list) == 1 and self.max_ms_reflex >= 1
             if use_ms:
                 plan = None
-                if self.tensor_cores:
+                if self.use_plans:
                     plan = self._plans.get(id(ch))
                     if plan is None:
                         plan = ObjectivePlan(ch["src_to_dst"], ch["src_to_ms{0}"],
