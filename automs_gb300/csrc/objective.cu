@@ -811,6 +811,129 @@ __global__ void k_tc_dw_sum(const float *GU, const float *dwp, int C, int S, int
   reinterpret_cast<float2 *>(grad_W)[i] = t;
 }
 
+// Streaming paths, after the streaming kernel: one CTA per 32 rows k of
+// [H_r; H_d] (lanes, loads coalesced over k), 32 warps.
+//   G_U[c, k] = sum_b P1[b][c][k] + (sum_b P2[b][c][k]) / ||masked||, the
+//     warps splitting the CTA partials b; every CTA derives 1/||masked|| from
+//     the loss partials (CTA 0 also writes the loss);
+//   dphi[k] = -sum_c Im(conj(G_U[c, k]) U[c, k]) for metasurface rows;
+//   dwp[blk][c][s] = sum over the CTA's metasurface rows of
+//     G_U[c, k] e^{-j phi'_k} conj(H_a[s, k]), warp w taking s = w, w + 32, ...
+// k_stream_dw then adds the CTAs' dwp and the H_d rows G_U[c, M + s].
+template <int CB>
+__global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int nparts,
+                                                      const float *Ppart, const double *lpart,
+                                                      const float *U, float *GU, float *dwp) {
+  constexpr int NW = 32;
+  const int K = M + a.S;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  __shared__ float inv_s;
+  __shared__ c2 r1[NW][CB][32], r2[NW][CB][32];
+  __shared__ c2 gv[CB][32];
+  if (warp == 0) {
+    double x = 0.0, z = 0.0;
+    for (int b = lane; b < nparts; b += 32) { x += lpart[2 * b]; z += lpart[2 * b + 1]; }
+    for (int o = 16; o > 0; o >>= 1) {
+      x += __shfl_xor_sync(0xffffffffu, x, o);
+      z += __shfl_xor_sync(0xffffffffu, z, o);
+    }
+    if (lane == 0) {
+      const double nrm = sqrt(z);
+      inv_s = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
+      if (blockIdx.x == 0 && a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
+    }
+  }
+  const float2 *P = reinterpret_cast<const float2 *>(Ppart);
+  const int kk = k < K ? k : K - 1;
+  c2 s1[CB], s2[CB];
+#pragma unroll
+  for (int c = 0; c < CB; c++) { s1[c] = {0.f, 0.f}; s2[c] = {0.f, 0.f}; }
+#pragma unroll 4
+  for (int b = warp; b < nparts; b += NW) {
+#pragma unroll
+    for (int c = 0; c < CB; c++) {
+      if (c >= a.C) continue;
+      const float2 u = __ldg(P + ((size_t)b * 2 * a.C + c) * K + kk);
+      s1[c].x += u.x;
+      s1[c].y += u.y;
+      if (CB > 1) {
+        const float2 v = __ldg(P + ((size_t)b * 2 * a.C + a.C + c) * K + kk);
+        s2[c].x += v.x;
+        s2[c].y += v.y;
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < CB; c++) { r1[warp][c][lane] = s1[c]; r2[warp][c][lane] = s2[c]; }
+  __syncthreads();
+  if (warp == 0) {
+    const float inv = inv_s;
+    c2 e = {1.f, 0.f};
+    const bool ms_row = k < M;
+    if (ms_row) {
+      const float pp = py_mod(__ldg(a.phi + k), a.max_phase);
+      sincosf(pp, &e.y, &e.x);
+    }
+    float dph = 0.f;
+#pragma unroll
+    for (int c = 0; c < CB; c++) {
+      c2 g = {0.f, 0.f};
+      if (c < a.C && k < K) {
+        c2 t1 = {0.f, 0.f}, t2 = {0.f, 0.f};
+#pragma unroll 8
+        for (int w = 0; w < NW; w++) {
+          t1.x += r1[w][c][lane].x; t1.y += r1[w][c][lane].y;
+          t2.x += r2[w][c][lane].x; t2.y += r2[w][c][lane].y;
+        }
+        g = {fmaf(t2.x, inv, t1.x), fmaf(t2.y, inv, t1.y)};
+        reinterpret_cast<float2 *>(GU)[(size_t)c * K + k] = make_float2(g.x, g.y);
+        if (ms_row) {
+          const c2 u = ld2(U, (size_t)c * M + k);
+          dph += g.x * u.y - g.y * u.x;  // Im(conj(g) u)
+        }
+      }
+      // g e^{-j phi'} of metasurface rows (zero elsewhere) for the dW sums
+      gv[c][lane] = ms_row && c < a.C ? c2{g.x * e.x + g.y * e.y, g.y * e.x - g.x * e.y}
+                                      : c2{0.f, 0.f};
+    }
+    if (ms_row && a.grad_phi) a.grad_phi[k] = -dph;
+  }
+  if (!a.grad_W) return;
+  __syncthreads();
+  for (int s2 = warp; s2 < a.S; s2 += NW) {
+    const c2 h = k < M ? ld2(a.Ha, (size_t)s2 * M + k) : c2{0.f, 0.f};
+#pragma unroll
+    for (int c = 0; c < CB; c++) {
+      if (c >= a.C) continue;
+      c2 d = {0.f, 0.f};
+      macc(d, gv[c][lane], h);
+      for (int o = 16; o > 0; o >>= 1) {
+        d.x += __shfl_xor_sync(0xffffffffu, d.x, o);
+        d.y += __shfl_xor_sync(0xffffffffu, d.y, o);
+      }
+      if (lane == 0)
+        reinterpret_cast<float2 *>(dwp)[((size_t)blockIdx.x * a.C + c) * a.S + s2] =
+            make_float2(d.x, d.y);
+    }
+  }
+}
+
+// grad_W[c, s] = G_U[c, M + s] + sum over the tail CTAs of dwp[blk][c][s]
+__global__ void k_stream_dw(const float *GU, const float *dwp, int nblk, int C, int S, int M,
+                            float *grad_W) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= C * S) return;
+  const int c = i / S, s2 = i % S, K = M + S;
+  float2 t = reinterpret_cast<const float2 *>(GU)[(size_t)c * K + M + s2];
+  for (int b = 0; b < nblk; b++) {
+    const float2 v = reinterpret_cast<const float2 *>(dwp)[(size_t)b * C * S + i];
+    t.x += v.x;
+    t.y += v.y;
+  }
+  reinterpret_cast<float2 *>(grad_W)[i] = t;
+}
+
 // grad_Y = G1 + G2 / ||masked||
 __global__ void k_grad_y(const float *G1, const float *G2, const float *scal, long long n,
                          float *out) {
@@ -892,21 +1015,27 @@ cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *U, float *Yp
 // capacity, max and mask and the two gradient parts, and (C) accumulates
 // P1[c,k] += sum_col G1[c,col] conj(H[k,col]) (and P2 for the norm term)
 // from the same shared-memory tile.  The per-CTA P1/P2 and loss partials are
-// reduced by k_stream_reduce; k_final then forms dphi and dL/dW.
+// reduced by k_stream_gu; k_tc_dphi and k_tc_dw_part / k_tc_dw_sum then form
+// dphi and dL/dW.
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
+// try_wait with a suspend-time hint: the thread sleeps until the phase
+// completes or the hint runs out instead of spinning (spinning warps took
+// issue slots from the other CTA on the SM); the 2 s bound is checked after
+// each wake-up
+constexpr uint32_t kSuspendNs = 1000000u;
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
   unsigned long long t0 = 0;
   for (uint32_t it = 0;; it++) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(kSuspendNs)
         : "memory");
     if (ok) return true;
     unsigned long long t;
@@ -1114,128 +1243,6 @@ __global__ void __launch_bounds__(256, 2)
   }
 }
 
-// final of the streaming path: one warp per row k of [H_r; H_d].
-// The warp reduces the row's CTA partials, G_U = sum P1 + (sum P2)/||masked||.
-// Metasurface rows write dphi = -sum_c Im(conj(G_U) U) (U recomputed) and add
-// G_U e^{-j phi'} conj(H_a[:, k]) to the CTA's dL/dW partial; H_d rows add
-// G_U itself.  The last CTA sums the CTA partials into grad_W, one warp per
-// entry.  Block 0 writes the loss.
-template <int CB>
-__global__ void __launch_bounds__(256) k_stream_final(ObjArgs a, int M, int nparts,
-                                                      const float *Ppart, const double *lpart,
-                                                      float *gw_part, unsigned *counter) {
-  extern __shared__ float2 gw_s[];  // [C * S] partial dL/dW of this CTA
-  __shared__ float inv_s;
-  __shared__ bool last;
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const int K = M + a.S;
-  const int k = blockIdx.x * 8 + warp;
-  const int CS = a.C * a.S;
-  const float2 *P = reinterpret_cast<const float2 *>(Ppart);
-  for (int i = t; i < CS; i += blockDim.x) gw_s[i] = make_float2(0.f, 0.f);
-  if (warp == 0) {
-    double x = 0, z = 0;
-    for (int b = lane; b < nparts; b += 32) { x += lpart[2 * b]; z += lpart[2 * b + 1]; }
-    for (int o = 16; o > 0; o >>= 1) {
-      x += __shfl_xor_sync(0xffffffffu, x, o);
-      z += __shfl_xor_sync(0xffffffffu, z, o);
-    }
-    if (lane == 0) {
-      const double nrm = sqrt(z);
-      inv_s = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
-      if (blockIdx.x == 0 && a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
-    }
-  }
-  __syncthreads();
-  const float inv = inv_s;
-  if (k < K) {
-    c2 gu[CB];
-#pragma unroll
-    for (int c = 0; c < CB; c++) {
-      c2 s1 = {0.f, 0.f}, s2 = {0.f, 0.f};
-      if (c < a.C) {
-#pragma unroll 4
-        for (int b = lane; b < nparts; b += 32) {
-          const float2 u = __ldcg(P + ((size_t)b * 2 * a.C + c) * K + k);
-          s1.x += u.x; s1.y += u.y;
-          if (CB > 1) {
-            const float2 v = __ldcg(P + ((size_t)b * 2 * a.C + a.C + c) * K + k);
-            s2.x += v.x; s2.y += v.y;
-          }
-        }
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        s1.x += __shfl_xor_sync(0xffffffffu, s1.x, o);
-        s1.y += __shfl_xor_sync(0xffffffffu, s1.y, o);
-        s2.x += __shfl_xor_sync(0xffffffffu, s2.x, o);
-        s2.y += __shfl_xor_sync(0xffffffffu, s2.y, o);
-      }
-      gu[c] = c2{fmaf(s2.x, inv, s1.x), fmaf(s2.y, inv, s1.y)};
-    }
-    if (k < M) {
-      c2 e;
-      const float pp = py_mod(__ldg(a.phi + k), a.max_phase);
-      sincosf(pp, &e.y, &e.x);
-      float sacc = 0.f;
-#pragma unroll
-      for (int c = 0; c < CB; c++) {
-        if (c >= a.C) continue;
-        // U[c,k] = (sum_s W[c,s] H_a[s,k]) e^{j phi'}, lanes over s
-        c2 acc = {0.f, 0.f};
-        for (int s2 = lane; s2 < a.S; s2 += 32)
-          mac(acc, ld2(a.W, (size_t)c * a.S + s2), ld2(a.Ha, (size_t)s2 * M + k));
-        for (int o = 16; o > 0; o >>= 1) {
-          acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-          acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-        }
-        c2 u = {0.f, 0.f};
-        mac(u, acc, e);
-        sacc += gu[c].x * u.y - gu[c].y * u.x;  // Im(conj(g) u)
-        const c2 gv = {gu[c].x * e.x + gu[c].y * e.y, gu[c].y * e.x - gu[c].x * e.y};
-        if (a.grad_W)
-          for (int s2 = lane; s2 < a.S; s2 += 32) {
-            c2 d = {0.f, 0.f};
-            macc(d, gv, ld2(a.Ha, (size_t)s2 * M + k));
-            atomicAdd(&gw_s[c * a.S + s2].x, d.x);
-            atomicAdd(&gw_s[c * a.S + s2].y, d.y);
-          }
-      }
-      if (lane == 0 && a.grad_phi) a.grad_phi[k] = -sacc;
-    } else if (a.grad_W && lane == 0) {
-#pragma unroll
-      for (int c = 0; c < CB; c++) {
-        if (c >= a.C) continue;
-        atomicAdd(&gw_s[c * a.S + (k - M)].x, gu[c].x);
-        atomicAdd(&gw_s[c * a.S + (k - M)].y, gu[c].y);
-      }
-    }
-  }
-  if (!a.grad_W) return;
-  __syncthreads();
-  for (int i = t; i < CS; i += blockDim.x)
-    reinterpret_cast<float2 *>(gw_part)[(size_t)blockIdx.x * CS + i] = gw_s[i];
-  __threadfence();
-  __syncthreads();
-  if (t == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  const float2 *gp = reinterpret_cast<const float2 *>(gw_part);
-  for (int i = warp; i < CS; i += 8) {
-    c2 acc = {0.f, 0.f};
-#pragma unroll 4
-    for (int b = lane; b < (int)gridDim.x; b += 32) {
-      const float2 u = __ldcg(gp + (size_t)b * CS + i);
-      acc.x += u.x; acc.y += u.y;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-    }
-    if (lane == 0) reinterpret_cast<float2 *>(a.grad_W)[i] = make_float2(acc.x, acc.y);
-  }
-  if (t == 0) *counter = 0u;  // ready for the next call
-}
 
 using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                               const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
@@ -1356,9 +1363,12 @@ cudaError_t launch_stream_k(const ObjArgs &a, const StreamPlan &pl, const CUtens
 }
 
 template <int CB>
+cudaError_t stream_tail(const ObjArgs &a, int M, int nparts, const float *U, const float *Pp,
+                        const double *lp, float *GU, float *dwp, cudaStream_t st);
+
+template <int CB>
 cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, float *Ppart,
-                       double *lpart, float *gw_part, unsigned *counter, unsigned *err,
-                       cudaStream_t st) {
+                       double *lpart, float *GU, float *dwp, unsigned *err, cudaStream_t st) {
   CUtensorMap mr, md;
   const float *Hr = M > 0 ? a.Hr : a.Hd;  // no metasurface: mapR is unused (Mbox = 0)
   if (!make_cmap(&mr, Hr, std::max(M, 1), a.R, pl.TR, pl.boxR) ||
@@ -1375,9 +1385,17 @@ cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, 
     default: e = launch_stream_k<CB, 2>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
   }
   if (e != cudaSuccess) return e;
-  const int nbf = (M + a.S + 7) / 8;
-  k_stream_final<CB><<<nbf, 256, sizeof(float2) * a.C * a.S, st>>>(a, M, pl.grid, Ppart, lpart,
-                                                                     gw_part, counter);
+  return stream_tail<CB>(a, M, pl.grid, U, Ppart, lpart, GU, dwp, st);
+}
+
+// after a streaming kernel: G_U, dphi and the dL/dW parts, then dL/dW
+template <int CB>
+cudaError_t stream_tail(const ObjArgs &a, int M, int nparts, const float *U, const float *Pp,
+                        const double *lp, float *GU, float *dwp, cudaStream_t st) {
+  const int K = M + a.S, nblk = (K + 31) / 32;
+  k_stream_tail<CB><<<nblk, 1024, 0, st>>>(a, M, nparts, Pp, lp, U, GU, dwp);
+  if (a.grad_W)
+    k_stream_dw<<<(a.C * a.S + 127) / 128, 128, 0, st>>>(GU, dwp, nblk, a.C, a.S, M, a.grad_W);
   return cudaGetLastError();
 }
 
@@ -1821,7 +1839,8 @@ ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
   size_t o = 0;
   L.inv = o; o += 256;                                    // control block (see header)
   L.Um = o; o += al(8 * (size_t)C * std::max(M, 1));      // U = (W H_a) e^{j phi'}
-  L.gw = o; o += al(8 * (size_t)std::max((M + 31) / 32, (M + S + 7) / 8) * C * S);  // dL/dW partials
+  L.gw = o;  // dL/dW partials (k_final CTAs, or the streaming tail CTAs)
+  o += al(8 * (size_t)std::max((M + 31) / 32, (M + S + 31) / 32) * C * S);
   L.U = o; o += al(8 * (size_t)sp.kspl * C * R);          // Y partials
   L.G1 = o; o += al(8 * (size_t)C * R);
   L.G2 = o; o += al(8 * (size_t)C * R);
@@ -1857,8 +1876,9 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
     float *Pp = reinterpret_cast<float *>(scratch + L.Pp);
     double *lp = reinterpret_cast<double *>(scratch + L.lp);
     unsigned *err = reinterpret_cast<unsigned *>(scratch + L.inv + 48);
-    if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Um, Pp, lp, gw, counter + 1, err, st);
-    return run_stream<2>(a, pl, M, Um, Pp, lp, gw, counter + 1, err, st);
+    float *GUs = reinterpret_cast<float *>(scratch + L.GUs);
+    if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Um, Pp, lp, GUs, gw, err, st);
+    return run_stream<2>(a, pl, M, Um, Pp, lp, GUs, gw, err, st);
   }
   switch (cbucket(a.C)) {
 #define CASE(CB) case CB: return run_cb<CB>(a, sp, M, Um, Ypart, G1, G2, part, counter, scal, GUp, gw, st);
@@ -1917,7 +1937,8 @@ cudaError_t plan_stream_create(ObjTcPlan *p, cudaStream_t st, ObjTcPlan **out) {
   p->oU = o; o += al(8 * (size_t)p->Cmax * M);
   p->oPp = o; o += al(8 * (size_t)p->tGrid * 2 * p->Cmax * K);
   p->oLp = o; o += al(16 * (size_t)p->tGrid);
-  p->oGwS = o; o += al(8 * (size_t)((K + 7) / 8) * p->Cmax * S);
+  p->oGwS = o; o += al(8 * (size_t)p->Cmax * K);           // G_U
+  p->oDw = o; o += al(8 * (size_t)((K + 31) / 32) * p->Cmax * S);  // dL/dW per tail CTA
   p->bytes = o;
   cudaError_t e = cudaMalloc(&p->mem, o);
   if (e != cudaSuccess) { delete p; return e; }
@@ -1991,10 +2012,9 @@ cudaError_t run_plan_stream(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st) {
     default: e = launch_stream_ht_k<CB, 2>(p, a, U, Pp, lp, err, st); break;
   }
   if (e != cudaSuccess) return e;
-  const int nbf = (M + a.S + 7) / 8;
-  k_stream_final<CB><<<nbf, 256, sizeof(float2) * a.C * a.S, st>>>(a, M, p->tGrid, Pp, lp, gw,
-                                                                     counter);
-  return cudaGetLastError();
+  (void)counter;
+  return stream_tail<CB>(a, M, p->tGrid, U, Pp, lp, gw, reinterpret_cast<float *>(p->mem + p->oDw),
+                         st);
 }
 }  // namespace
 
