@@ -99,6 +99,24 @@ struct ams_scene {
     }                                                                                    \
   } while (0)
 
+namespace {
+// Timing between two recorded events, 0 when it cannot be read.  The error
+// such a call returns is also left as the thread's last error, which a later
+// cudaGetLastError() (after our own launches) would misreport: clear it.
+float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    (void)cudaGetLastError();
+    ms = 0.f;
+  }
+  return ms;
+}
+// An entry point starts with no pending error from runtime calls made
+// elsewhere on this thread (its own launches are checked with
+// cudaGetLastError()).
+void clear_stale_error() { (void)cudaGetLastError(); }
+}  // namespace
+
 extern "C" {
 
 const char *ams_version(void) { return "automs-gb300 0.1 (sm_103a)"; }
@@ -106,6 +124,7 @@ const char *ams_version(void) { return "automs-gb300 0.1 (sm_103a)"; }
 ams_status ams_scene_create(const float *tris, int n_tri, const int *mat, const float *mat_prop,
                             int n_mat, void *stream, ams_scene **out, char *errbuf,
                             size_t errlen) {
+  clear_stale_error();
   if (!out) { set_err(errbuf, errlen, "out is NULL"); return AMS_ERR_ARG; }
   *out = nullptr;
   if (n_tri < 0 || n_mat < 0 || (n_tri > 0 && (!tris || !mat)) || (n_mat > 0 && !mat_prop) ||
@@ -148,12 +167,20 @@ ams_status ams_scene_create(const float *tris, int n_tri, const int *mat, const 
         set_err(errbuf, errlen, "mat[%d] = %d is outside [0, %d)", i, hm[i], n_mat);
         return fail(AMS_ERR_ARG);
       }
-    cudaMemcpyAsync(s->tris, tris, sizeof(float) * 9 * (size_t)n_tri, cudaMemcpyDeviceToDevice, st);
-    cudaMemcpyAsync(s->mat, mat, sizeof(int) * (size_t)n_tri, cudaMemcpyDeviceToDevice, st);
+    if ((e = cudaMemcpyAsync(s->tris, tris, sizeof(float) * 9 * (size_t)n_tri,
+                             cudaMemcpyDeviceToDevice, st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s->mat, mat, sizeof(int) * (size_t)n_tri, cudaMemcpyDeviceToDevice,
+                             st)) != cudaSuccess) {
+      set_err(errbuf, errlen, "copying the scene arrays: %s", cudaGetErrorString(e));
+      return fail(AMS_ERR_CUDA);
+    }
   }
-  if (n_mat > 0)
-    cudaMemcpyAsync(s->mat_prop, mat_prop, sizeof(float) * 19 * (size_t)n_mat,
-                    cudaMemcpyDeviceToDevice, st);
+  if (n_mat > 0 &&
+      (e = cudaMemcpyAsync(s->mat_prop, mat_prop, sizeof(float) * 19 * (size_t)n_mat,
+                           cudaMemcpyDeviceToDevice, st)) != cudaSuccess) {
+    set_err(errbuf, errlen, "copying mat_prop: %s", cudaGetErrorString(e));
+    return fail(AMS_ERR_CUDA);
+  }
   if ((e = s->ws.ensure(lbvh_scratch_bytes(n_tri) + 1024)) != cudaSuccess) {
     set_err(errbuf, errlen, "BVH scratch: %s", cudaGetErrorString(e));
     return fail(AMS_ERR_OOM);
@@ -215,6 +242,7 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
                              int s1, const float *dst, int n0, int n1, const float *src_aabb_in,
                              const float *dst_aabb_in, float *result, ams_stats *stats,
                              void *stream, char *errbuf, size_t errlen) {
+  clear_stale_error();
   if (!S) { set_err(errbuf, errlen, "scene is NULL"); return AMS_ERR_ARG; }
   ams_status v = validate(p, s0, s1, n0, n1, errbuf, errlen);
   if (v != AMS_OK) return v;
@@ -345,9 +373,7 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
           set_err(errbuf, errlen, "stage 2 device error flags 0x%x", S->hc->err);
           return (S->hc->err & AMS_DERR_ACC_RANGE) ? AMS_ERR_NUMERIC : AMS_ERR_CAPACITY;
         }
-        float kms = 0.f;
-        cudaEventElapsedTime(&kms, S->k2[0], S->k2[1]);
-        ms_k2 += kms;
+        ms_k2 += elapsed_ms(S->k2[0], S->k2[1]);
         if (S->hc->ctr[5] != n_new) {
           set_err(errbuf, errlen, "task count mismatch (%llu listed, %llu expected)",
                   S->hc->ctr[5], n_new);
@@ -372,20 +398,18 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
       stats->rounds = rounds;
       stats->tasks = total_tasks;
       stats->overflow = overflow;
-      cudaEventElapsedTime(&stats->ms_bvh, ev[0], ev[1]);
-      cudaEventElapsedTime(&stats->ms_stage1, ev[1], ev[2]);
-      cudaEventElapsedTime(&stats->ms_stage2, ev[2], ev[3]);
-      cudaEventElapsedTime(&stats->ms_total, ev[0], ev[3]);
+      stats->ms_bvh = elapsed_ms(ev[0], ev[1]);
+      stats->ms_stage1 = elapsed_ms(ev[1], ev[2]);
+      stats->ms_stage2 = elapsed_ms(ev[2], ev[3]);
+      stats->ms_total = elapsed_ms(ev[0], ev[3]);
       stats->workspace_bytes = S->ws.high + S->tasks.high;
       stats->segments_fwd = S->hc->ctr[8];
       stats->segments_bwd = S->hc->ctr[9];
       stats->ms_stage2_kernel = ms_k2;
     }
     if (p->log_level > 0) {
-      float a = 0, b = 0, c = 0;
-      cudaEventElapsedTime(&a, ev[0], ev[1]);
-      cudaEventElapsedTime(&b, ev[1], ev[2]);
-      cudaEventElapsedTime(&c, ev[2], ev[3]);
+      const float a = elapsed_ms(ev[0], ev[1]), b = elapsed_ms(ev[1], ev[2]),
+                  c = elapsed_ms(ev[2], ev[3]);
       fprintf(stderr,
               "[ams] bvh %.3f ms, stage1 %.3f ms (%llu records, %llu unique, %llu paths), "
               "stage2 %.3f ms (%llu rounds, %llu tasks), rays %llu ok / %llu failed\n",
@@ -407,6 +431,7 @@ ams_status ams_launch_pathtrace(float *result, const float *src, int s0, int s1,
                                 const float *dst_dir, int log_level, int src_bptype,
                                 int dst_bptype, int dst_gridsize, double src_r, double dst_r,
                                 ams_stats *stats, char *errbuf, size_t errlen) {
+  clear_stale_error();
   if (!src_dir || !dst_dir) { set_err(errbuf, errlen, "src_dir/dst_dir are NULL"); return AMS_ERR_ARG; }
   ams_trace_params p{};
   p.samples_per_launch = samples_per_launch;
@@ -434,6 +459,7 @@ ams_status ams_launch_pathtrace(float *result, const float *src, int s0, int s1,
 
 ams_status ams_trace_export_paths(ams_scene *S, int32_t *host_out, int max_paths, int *n_out,
                                   char *errbuf, size_t errlen) {
+  clear_stale_error();
   if (!S || !n_out || (max_paths > 0 && !host_out)) {
     set_err(errbuf, errlen, "bad arguments");
     return AMS_ERR_ARG;
@@ -531,6 +557,7 @@ ams_status ams_objective_fwd_bwd(const float *H_d, const float *H_a, const float
                                  int R, int C, float w, const uint8_t *drop, float *loss,
                                  float *grad_W, float *grad_phi, float *grad_Y, float *recv_amp,
                                  void *stream, char *errbuf, size_t errlen) {
+  clear_stale_error();
   ams_status v = obj_validate(H_d, H_a, H_r, phi, max_phase, W, S, M, R, C, errbuf, errlen);
   if (v != AMS_OK) return v;
   if (!loss) { set_err(errbuf, errlen, "loss output is NULL"); return AMS_ERR_ARG; }
@@ -551,6 +578,7 @@ ams_status ams_objective_fwd_bwd_noalloc(const float *H_d, const float *H_a, con
                                          float *loss, float *grad_W, float *grad_phi,
                                          float *grad_Y, float *recv_amp, void *stream,
                                          char *errbuf, size_t errlen) {
+  clear_stale_error();
   ams_status v = obj_validate(H_d, H_a, H_r, phi, max_phase, W, S, M, R, C, errbuf, errlen);
   if (v != AMS_OK) return v;
   if (!loss) { set_err(errbuf, errlen, "loss output is NULL"); return AMS_ERR_ARG; }
@@ -583,6 +611,7 @@ struct ams_objective_plan {
 ams_status ams_objective_plan_create(const float *H_d, const float *H_a, const float *H_r, int S,
                                      int M, int R, int C_max, void *stream,
                                      ams_objective_plan **out, char *errbuf, size_t errlen) {
+  clear_stale_error();
   if (!out) { set_err(errbuf, errlen, "out is NULL"); return AMS_ERR_ARG; }
   *out = nullptr;
   if (!H_d || !H_a || !H_r) {
@@ -610,6 +639,7 @@ ams_status ams_objective_plan_fwd_bwd(ams_objective_plan *plan, const float *phi
                                       float *loss, float *grad_W, float *grad_phi, float *grad_Y,
                                       float *recv_amp, void *stream, char *errbuf,
                                       size_t errlen) {
+  clear_stale_error();
   if (!plan || !plan->p) { set_err(errbuf, errlen, "plan is NULL"); return AMS_ERR_ARG; }
   if (!phi || !W || !loss) { set_err(errbuf, errlen, "phi, W and loss are required"); return AMS_ERR_ARG; }
   if (C <= 0 || C > plan->Cmax) {
@@ -641,6 +671,7 @@ ams_status ams_objective_recv(const float *H_d, const float *H_a, const float *H
                               const float *phi, float max_phase, const float *W, int S, int M,
                               int R, int C, float *recv_amp, void *stream, char *errbuf,
                               size_t errlen) {
+  clear_stale_error();
   ams_status v = obj_validate(H_d, H_a, H_r, phi, max_phase, W, S, M, R, C, errbuf, errlen);
   if (v != AMS_OK) return v;
   if (!recv_amp) { set_err(errbuf, errlen, "recv_amp is NULL"); return AMS_ERR_ARG; }
@@ -656,6 +687,7 @@ ams_status ams_objective_recv(const float *H_d, const float *H_a, const float *H
 
 ams_status ams_coverage_db(const float *H, int S, int R, float threshold, float offset, float *out,
                            void *stream, char *errbuf, size_t errlen) {
+  clear_stale_error();
   if (!H || !out || S <= 0 || R <= 0) { set_err(errbuf, errlen, "bad arguments"); return AMS_ERR_ARG; }
   CK(coverage_db_run(H, S, R, threshold, offset, out, (cudaStream_t)stream));
   return AMS_OK;
@@ -705,6 +737,7 @@ extern "C" {
 ams_status ams_gemm_bf16(const void *A, const void *B, int M, int N, int K, const float *bias,
                          int relu, float *C32, void *C16, void *stream, char *errbuf,
                          size_t errlen) {
+  clear_stale_error();
   if (!A || !B || (!C32 && !C16)) { set_err(errbuf, errlen, "null operand"); return AMS_ERR_ARG; }
   if (M <= 0 || N <= 0 || K <= 0 || M % 128 || N % 64 || K % 64) {
     set_err(errbuf, errlen, "need M %% 128 == 0, N %% 64 == 0, K %% 64 == 0 (M=%d N=%d K=%d)", M,
@@ -744,6 +777,7 @@ ams_status ams_gemm_bf16(const void *A, const void *B, int M, int N, int K, cons
 
 ams_status ams_mlp_create(const int *dims, int n_dims, int max_batch, unsigned long long seed,
                           void *stream, ams_mlp **out, char *errbuf, size_t errlen) {
+  clear_stale_error();
   if (!out || !dims || n_dims < 2 || n_dims > kMlpMaxLayers + 1 || max_batch <= 0) {
     set_err(errbuf, errlen, "bad MLP shape");
     return AMS_ERR_ARG;
@@ -821,6 +855,7 @@ void ams_mlp_destroy(ams_mlp *mlp) { delete mlp; }
 
 ams_status ams_mlp_forward(ams_mlp *m, const float *X, int B, float *Y, void *stream, char *errbuf,
                            size_t errlen) {
+  clear_stale_error();
   if (!m || !X || !Y || B <= 0 || B > m->dev.max_bp) {
     set_err(errbuf, errlen, "bad MLP forward arguments (B=%d)", B);
     return AMS_ERR_ARG;
@@ -831,6 +866,7 @@ ams_status ams_mlp_forward(ams_mlp *m, const float *X, int B, float *Y, void *st
 
 ams_status ams_mlp_train_step(ams_mlp *m, const float *X, const float *T, int B, float lr,
                               float *loss, void *stream, char *errbuf, size_t errlen) {
+  clear_stale_error();
   if (!m || !X || !T || B <= 0 || B > m->dev.max_bp || !(lr >= 0.f)) {
     set_err(errbuf, errlen, "bad MLP training arguments (B=%d)", B);
     return AMS_ERR_ARG;
@@ -863,6 +899,7 @@ static void mlp_param_copy(MlpDev &d, float *flat, bool to_flat, bool grads, cud
 
 ams_status ams_mlp_gradients(ams_mlp *m, const float *X, const float *T, int B, float *loss,
                              float *grads, void *stream, char *errbuf, size_t errlen) {
+  clear_stale_error();
   if (!m || !X || !T || !grads || B <= 0 || B > m->dev.max_bp) {
     set_err(errbuf, errlen, "bad MLP gradient arguments");
     return AMS_ERR_ARG;

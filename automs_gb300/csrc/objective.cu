@@ -2032,7 +2032,10 @@ cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr
   p->K2p = round_up(2LL * R, 64);
   p->Mp = round_up(2LL * Cmax, tcg::BM);
   const int sms = sm_count();
-  if (Cmax <= 2) return plan_stream_create(p, st, out);
+  // stream mode when the streaming kernel's per-thread rows cover K (16 rows
+  // a thread for one code, 8 for two); otherwise the tensor-core mode
+  const int kpt = (p->K + 255) / 256;
+  if (Cmax <= 2 && kpt <= (Cmax == 1 ? 16 : 8)) return plan_stream_create(p, st, out);
   pick_split((p->Rp / tcg::BN) * (p->Mp / tcg::BM), p->Kp / tcg::BK, sms, p->ksy, p->kpy);
   pick_split((p->Np / tcg::BN) * (p->Mp / tcg::BM), p->K2p / tcg::BK, sms, p->ksg, p->kpg);
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };

@@ -246,3 +246,82 @@ def screening_report(study, mlp, pool_params, pool_gain, top_frac=0.05, t_trial=
         "plain_configs_per_s": 1.0 / t_trial,
         "screened_configs_per_s": n / (t_rank + k * t_trial),
     }
+
+
+def batch_evaluate(cfg, indices=None, workers=4, opt_steps=20, lr=0.3):
+    """Batched hyper-configs (scenes.batch_config): for each placement the
+    AP->Rx channel with the metasurface as a blackhole, the AP->MS and MS->Rx
+    channels (build_channels, go.py:1135-1247), then opt_steps Adam steps of
+    the phase map on an evaluation plan (optimize_model, go.py:296-336, with
+    C = 1 and w = 1/R).
+
+    Placements run on `workers` host threads, each with its own CUDA stream
+    and scene handle, so one placement's flood-fill round trips overlap the
+    others' kernels.  Returns per-placement results and the wall time."""
+    import concurrent.futures as cf
+    import threading
+
+    from . import objective as obj
+    from . import scenes as sc_mod
+
+    if indices is None:
+        indices = list(range(len(cfg["placements"])))
+    src, dst = cfg["src"], cfg["dst"]
+    R = dst.shape[0] * dst.shape[1]
+    S = src.shape[0] * src.shape[1]
+    prm = cfg["prm"]
+    none = (0.0, 0.0, 0.0)
+    local = threading.local()
+    scenes_made = []
+    lock = threading.Lock()
+
+    def work(pi):
+        if not hasattr(local, "scene"):
+            local.stream = torch.cuda.Stream()
+            with torch.cuda.stream(local.stream):
+                local.scene = tracer.Scene(cfg["tris"], cfg["mat"], cfg["mat_prop"])
+            with lock:
+                scenes_made.append(local.scene)
+        pl = cfg["placements"][pi]
+        pos, k = pl["pos"], tuple(float(x) for x in pl["normal"])
+        with torch.cuda.stream(local.stream):
+            t0 = time.perf_counter()
+            bh = tracer.Scene(*sc_mod.with_blackholes(cfg["tris"], cfg["mat"], cfg["mat_prop"],
+                                                      [pl["blackhole"]]))
+            rd, sd = bh.trace(src, dst, tracer.params_from_dict(prm(2, 0, cfg["ap_dir"], none)))
+            bh.close()
+            ra, sa = local.scene.trace(src, pos, tracer.params_from_dict(prm(2, 1, cfg["ap_dir"], k)))
+            rr, sr = local.scene.trace(pos, dst, tracer.params_from_dict(prm(1, 0, k, none)))
+            Hd, Ha, Hr = (torch.view_as_complex(x) for x in (rd, ra, rr))
+            t1 = time.perf_counter()
+            M = Ha.shape[1]
+            plan = obj.ObjectivePlan(Hd, Ha, Hr, c_max=1)
+            w = torch.ones(1, S, dtype=torch.complex64, device="cuda") / math.sqrt(S)
+            phi = torch.zeros(M, device="cuda", requires_grad=True)
+            opt = torch.optim.Adam([phi], lr=lr)
+            first = last = None
+            for _ in range(opt_steps):
+                loss = obj.capacity_objective(w, Hd, Ha, Hr, phi, 2 * math.pi, 1.0 / R, plan=plan)
+                loss.backward()
+                opt.step()
+                opt.zero_grad()
+                lv = loss.detach()
+                first = lv if first is None else first
+                last = lv
+            first_v, last_v = float(first), float(last)
+            plan.close()
+            local.stream.synchronize()
+            t2 = time.perf_counter()
+        return dict(index=pi, size=pl["size"], M=M, rx_paths=sd["rx_paths"] + sa["rx_paths"] + sr["rx_paths"],
+                    ms_to_rx_paths=sr["rx_paths"], t_trace=t1 - t0, t_opt=t2 - t1,
+                    loss_first=first_v, loss_last=last_v)
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        res = list(ex.map(work, indices))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    for s_ in scenes_made:
+        s_.close()
+    return res, wall

@@ -228,6 +228,118 @@ def channel_ms_config(name="ms-256", seed=0):
                 })
 
 
+def multiroom_scene(target_tris=200_000, rooms=(3, 3), seed=0, height=3.0):
+    """Seeded building of rooms x rooms rooms, each side U[6, 15] m, 3 m tall.
+
+    Outer shell (floor, ceiling, four walls) and interior walls on the room
+    boundaries, each wall segment with a 1 m wide, 2.1 m tall door gap;
+    floor-standing boxes (footprint U[0.2, 1.5]^2, height U[0.3, 2.0]) with
+    5x4 quads per face are added room by room until the scene has about
+    target_tris triangles.  Materials: floor, ceiling, walls, then one per
+    box, reflection coefficients U[0.3, 0.7] over all 19 bins.
+    Returns tris, mat, mat_prop, and the room grid edges (xs, ys)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    xs = np.concatenate([[0.0], np.cumsum(rng.uniform(6.0, 15.0, rooms[0]))])
+    ys = np.concatenate([[0.0], np.cumsum(rng.uniform(6.0, 15.0, rooms[1]))])
+    X, Y, Z = xs[-1], ys[-1], height
+    tris, mats = [], []
+    props = [rng.uniform(0.3, 0.7) for _ in range(3)]
+    ez = np.array([0.0, 0.0, Z])
+    floor = _quad_grid(np.zeros(3), np.array([X, 0, 0.0]), np.array([0, Y, 0.0]), 8, 8)
+    ceil = _quad_grid(ez, np.array([X, 0, 0.0]), np.array([0, Y, 0.0]), 8, 8)
+    tris += floor + ceil
+    mats += [0] * len(floor) + [1] * len(ceil)
+
+    def wall(p0, p1, door):
+        """Vertical wall from p0 to p1 (floor points); door: gap centre
+        fraction or None."""
+        p0, p1 = np.asarray(p0, float), np.asarray(p1, float)
+        L = np.linalg.norm(p1 - p0)
+        u = (p1 - p0) / L
+        out = []
+        if door is None:
+            out += _quad_grid(p0, p1 - p0, ez, 4, 2)
+        else:
+            c = door * L
+            a, b = max(c - 0.5, 0.0), min(c + 0.5, L)
+            if a > 0:
+                out += _quad_grid(p0, u * a, ez, 2, 2)
+            if b < L:
+                out += _quad_grid(p0 + u * b, u * (L - b), ez, 2, 2)
+            out += _quad_grid(p0 + u * a + np.array([0, 0, 2.1]), u * (b - a),
+                              np.array([0, 0, Z - 2.1]), 1, 1)
+        return out
+    w = []
+    w += wall((0, 0, 0), (X, 0, 0), None) + wall((0, Y, 0), (X, Y, 0), None)
+    w += wall((0, 0, 0), (0, Y, 0), None) + wall((X, 0, 0), (X, Y, 0), None)
+    for i in range(1, len(xs) - 1):          # interior walls x = xs[i]
+        for j in range(len(ys) - 1):
+            w += wall((xs[i], ys[j], 0), (xs[i], ys[j + 1], 0), rng.uniform(0.2, 0.8))
+    for j in range(1, len(ys) - 1):          # interior walls y = ys[j]
+        for i in range(len(xs) - 1):
+            w += wall((xs[i], ys[j], 0), (xs[i + 1], ys[j], 0), rng.uniform(0.2, 0.8))
+    tris += w
+    mats += [2] * len(w)
+    per_box = 12 * 5 * 4
+    n_boxes = max(0, (target_tris - len(tris)) // per_box)
+    nr = (len(xs) - 1) * (len(ys) - 1)
+    for bidx in range(n_boxes):
+        r = bidx % nr
+        i, j = r % (len(xs) - 1), r // (len(xs) - 1)
+        sx, sy = rng.uniform(0.2, 1.5, size=2)
+        h = rng.uniform(0.3, 2.0)
+        cx = rng.uniform(xs[i] + 0.3, xs[i + 1] - 0.3)
+        cy = rng.uniform(ys[j] + 0.3, ys[j + 1] - 0.3)
+        lo = np.array([max(cx - sx / 2, xs[i] + 0.05), max(cy - sy / 2, ys[j] + 0.05), 0.0])
+        hi = np.array([min(cx + sx / 2, xs[i + 1] - 0.05), min(cy + sy / 2, ys[j + 1] - 0.05), h])
+        bt = box_tris(lo, hi, (5, 4))
+        tris += bt
+        mats += [3 + bidx] * len(bt)
+        props.append(rng.uniform(0.3, 0.7))
+    tris = np.asarray(tris, np.float32)
+    mat = np.asarray(mats, np.int32)
+    mat_prop = np.repeat(np.asarray(props, np.float32)[:, None], 19, axis=1)
+    return tris, mat, mat_prop, xs, ys
+
+
+def batch_config(n_place=64, seed=0, target_tris=200_000, n_rx=256, launch=1000):
+    """Batched hyper-configs: a multi-room building (multiroom_scene), a
+    16-element AP in the middle room at 2.5 m facing +y, an n_rx x n_rx Rx
+    grid over the footprint at 1.5 m, and n_place metasurfaces of n x n
+    elements (n uniform over 16, 24, ..., 64) at lambda/2 on seeded outer-wall
+    positions facing into the building, 1 mm off the wall."""
+    rng = np.random.Generator(np.random.PCG64(1000 + seed))
+    tris, mat, mat_prop, xs, ys = multiroom_scene(target_tris, seed=seed)
+    X, Y = xs[-1], ys[-1]
+    lam = WAVE_LEN_60GHZ
+    ci, cj = (len(xs) - 1) // 2, (len(ys) - 1) // 2
+    ap = ((xs[ci] + xs[ci + 1]) / 2, (ys[cj] + ys[cj + 1]) / 2, 2.5)
+    src = ula(ap, (1, 0, 0), 16, lam / 2)
+    dst = rx_grid(0.25, X - 0.25, n_rx, 0.25, Y - 0.25, n_rx, 1.5)
+    walls = [((0.0, 0.0), (1.0, 0.0), (0.0, 1.0), X),       # y = 0, normal +y
+             ((0.0, Y), (1.0, 0.0), (0.0, -1.0), X),         # y = Y, normal -y
+             ((0.0, 0.0), (0.0, 1.0), (1.0, 0.0), Y),        # x = 0, normal +x
+             ((X, 0.0), (0.0, 1.0), (-1.0, 0.0), Y)]         # x = X, normal -x
+    place = []
+    for _ in range(n_place):
+        w = int(rng.integers(0, 4))
+        (ox, oy), (ux, uy), (nx, ny), L = walls[w]
+        n = int(rng.choice(np.arange(16, 65, 8)))
+        t = float(rng.uniform(1.0, L - 1.0))
+        z = float(rng.uniform(1.0, 2.0))
+        c = (ox + ux * t + nx * 1e-3, oy + uy * t + ny * 1e-3, z)
+        pos, quad, k = metasurface(c, (nx, ny, 0.0), (0.0, 0.0, -1.0), n, lam / 2)
+        place.append(dict(wall=w, size=n, pos=pos, blackhole=quad, normal=k))
+
+    def prm(sbp, dbp, sdir, ddir):
+        return dict(samples_per_launch=1, launch_x=launch, launch_y=launch, wave_len=lam,
+                    max_reflection=2, reserve_size=100, src_bptype=sbp, dst_bptype=dbp,
+                    dst_gridsize=5, src_r=0.5e-5, dst_r=0.06, src_dir=list(map(float, sdir)),
+                    dst_dir=list(map(float, ddir)))
+    return dict(tris=tris, mat=mat, mat_prop=mat_prop, src=src, dst=dst, placements=place,
+                prm=prm, ap_dir=(0.0, 1.0, 0.0))
+
+
 # ----------------------------------------------------------- STL scenes
 def read_stl(path):
     """Binary STL triangles as float32 [N, 3, 3] (what numpy-stl's

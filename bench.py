@@ -422,6 +422,36 @@ def surrogate_bench(torch, n_train=400, n_pool=200, top_frac=0.05):
                        "fit_loss_first_last": [hist[0], hist[-1]]}}
 
 
+def batch_bench(torch, n_place=64, workers=4, opt_steps=20):
+    """Batched hyper-configs: n_place metasurface placements (16x16 to 64x64
+    elements) on the outer walls of a seeded ~200k-triangle multi-room
+    building, 256x256 Rx grid, 1000x1000 launches, 2 reflections; per
+    placement the AP->Rx (metasurface as blackhole), AP->MS and MS->Rx traces
+    and opt_steps objective+adjoint Adam steps on an evaluation plan.
+    Placements run on `workers` host threads with one CUDA stream each."""
+    from automs_gb300 import placement, scenes
+    cfg = scenes.batch_config(n_place=n_place)
+    # warm-up: one small placement (library load, first launches)
+    small = min(range(n_place), key=lambda i: cfg["placements"][i]["size"])
+    placement.batch_evaluate(cfg, [small], workers=1, opt_steps=2)
+    res, wall = placement.batch_evaluate(cfg, list(range(n_place)), workers=workers,
+                                         opt_steps=opt_steps)
+    sizes = sorted({r["size"] for r in res})
+    by_size = {str(n): {"count": sum(1 for r in res if r["size"] == n),
+                        "mean_trace_s": float(np.mean([r["t_trace"] for r in res if r["size"] == n])),
+                        "mean_opt_s": float(np.mean([r["t_opt"] for r in res if r["size"] == n]))}
+               for n in sizes}
+    paths = sum(r["rx_paths"] for r in res)
+    improved = sum(1 for r in res if r["loss_last"] < r["loss_first"])
+    return {"metric": "batched hyper-configs/s (trace + objective+adjoint)", "value": n_place / wall,
+            "unit": "configs/s", "wall_s": wall, "rx_paths_per_s": paths / wall,
+            "config": {"workload": "multi-room building, 199,976 triangles, 16-element AP, "
+                                   "256x256 Rx, 1000x1000 launch, 2 reflections",
+                       "placements": n_place, "sizes": "16x16 to 64x64 (step 8)",
+                       "workers": workers, "adam_steps": opt_steps},
+            "by_size": by_size, "placements_with_lower_loss": improved}
+
+
 def channel_ms_bench(torch, warmup, steps, flush):
     """Channel set with one 32x32 metasurface on a 50k-triangle scene, 256x256
     Rx grid, 3 reflections, 1000x1000 launches: the AP->Rx, AP->MS and MS->Rx
@@ -526,8 +556,10 @@ def main():
     ap.add_argument("--no-secondary", action="store_true",
                     help="skip the codebook, channel-set and surrogate legs")
     ap.add_argument("--only", default="all",
-                    choices=["all", "tracer", "objective", "ms", "codes", "surrogate"],
+                    choices=["all", "tracer", "objective", "ms", "codes", "surrogate", "batch"],
                     help="profiling aid: run only the named timed loop")
+    ap.add_argument("--batch-n", type=int, default=64, help="placements of the batch leg")
+    ap.add_argument("--batch-workers", type=int, default=4)
     ap.add_argument("--codes-r", type=int, default=0, choices=[0, 4096, 65536],
                     help="profiling aid: run the codebook leg at one Rx count only")
     ap.add_argument("--launch", type=int, default=0,
@@ -556,6 +588,9 @@ def main():
         flushbuf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
         print(json.dumps(channel_ms_bench(torch, 1, max(1, args.steps),
                                           lambda: flushbuf.fill_(1.0))))
+        return
+    if args.only == "batch":
+        print(json.dumps(batch_bench(torch, n_place=args.batch_n, workers=args.batch_workers)))
         return
     if args.only == "surrogate":
         print(json.dumps(surrogate_bench(torch)))
@@ -658,6 +693,7 @@ def main():
         secondary.append(objective_codes_bench(torch, R=65536, nset=1))
         secondary.append(channel_ms_bench(torch, 1, 1, flush))
         secondary.append(surrogate_bench(torch))
+        secondary.append(batch_bench(torch))
 
     if rank != 0:
         if world > 1:

@@ -180,9 +180,10 @@ ams_status ams_objective_fwd_bwd_noalloc(
  * of ams_objective_fwd_bwd (the channels come from the plan); calls on one
  * plan must not overlap.  The plan owns about 8 (R (M+S) + (M+S) R) bytes of
  * device memory (ams_objective_plan_bytes).  A plan made with C_max <= 2
- * instead holds one FP32 copy of [H_r; H_d] transposed to [R][M+S] and runs
- * the single-pass streaming kernels over it (each tile of Rx is one
- * contiguous block); it does not produce grad_Y (AMS_ERR_ARG). */
+ * (and M+S <= 4096 for one code, 2048 for two) instead holds one FP32 copy
+ * of [H_r; H_d] transposed to [R][M+S] and runs the single-pass streaming
+ * kernels over it (each tile of Rx is one contiguous block); it does not
+ * produce grad_Y (AMS_ERR_ARG). */
 typedef struct ams_objective_plan ams_objective_plan;
 ams_status ams_objective_plan_create(const float *H_d, const float *H_a,
                                      const float *H_r, int S, int M, int R,

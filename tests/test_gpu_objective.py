@@ -245,6 +245,33 @@ def test_tensor_core_plan_matches_cuda_core_path(obj):
     plan.close()
 
 
+def test_plan_with_long_columns_uses_tensor_cores(obj):
+    """C_max = 1 with M + S above the streaming kernel's 4096 rows: the plan
+    falls back to the tensor-core mode and still matches the oracle."""
+    rng = np.random.Generator(np.random.PCG64(21))
+    S, M, R = 16, 4096, 256
+    ch = {"src_to_dst": cases._cn(rng, (S, R)), "src_to_ms{0}": cases._cn(rng, (S, M)),
+          "ms{0}_to_dst": cases._cn(rng, (M, R))}
+    c = dict(channels=ch, theta=rng.uniform(0, 2 * np.pi, size=(1, S)).astype(np.float32),
+             phi=[rng.uniform(0, 2 * np.pi, size=M).astype(np.float32)], n_ms=1, code_num=1,
+             w=1.0 / R, max_phase_deg=360.0)
+    ch, theta_np, A, drop, mp = _tc_inputs(c)
+    Hd, Ha, Hr = ch["src_to_dst"], ch["src_to_ms{0}"], ch["ms{0}_to_dst"]
+    phi = c["phi"][0]
+    loss_o, gth_o, gphi_o, ex = OO.objective(Hd, Ha, Hr, phi, theta_np, A, c["w"], drop, mp)
+    plan = obj.ObjectivePlan(cuda(Hd), cuda(Ha), cuda(Hr), c_max=1)
+    theta = cuda(theta_np).requires_grad_(True)
+    W = cuda(A.astype(np.float32)) * torch.exp(-1j * theta)
+    ph = cuda(phi).requires_grad_(True)
+    loss = obj.capacity_objective(W, cuda(Hd), cuda(Ha), cuda(Hr), ph, mp, c["w"], cuda(drop),
+                                  plan=plan)
+    loss.backward()
+    np.testing.assert_allclose(float(loss), loss_o, rtol=1e-4)
+    gp = ph.grad.cpu().numpy()
+    np.testing.assert_allclose(gp, gphi_o, rtol=1e-3, atol=1e-3 * np.abs(gphi_o).max())
+    plan.close()
+
+
 def test_tensor_core_plan_errors(obj):
     from automs_gb300._lib import AmsError
     c = cases.objective_case("c30")
