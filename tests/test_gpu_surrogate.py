@@ -34,3 +34,18 @@ def test_surrogate_screening_gains():
                                         surrogate=Denorm())
     assert len(cands) == 600
     net.close()
+
+
+def test_batched_placements_small():
+    """The batched hyper-config driver on a small building: every placement
+    is traced and optimised; channels have the expected shapes."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from automs_gb300 import placement, scenes
+    cfg = scenes.batch_config(n_place=4, target_tris=8_000, n_rx=32, launch=96)
+    res, wall = placement.batch_evaluate(cfg, workers=2, opt_steps=3)
+    assert len(res) == 4 and wall > 0
+    for r, p in zip(sorted(res, key=lambda x: x["index"]), cfg["placements"]):
+        assert r["M"] == p["size"] ** 2
+        assert np.isfinite(r["loss_first"]) and np.isfinite(r["loss_last"])
+        assert r["loss_last"] <= r["loss_first"] + 1e-6 * abs(r["loss_first"])

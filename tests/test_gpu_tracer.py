@@ -123,6 +123,27 @@ def test_full_coverage_parity_with_oracle(tracer):
     assert rel(H, Ho) < 1e-5
 
 
+def test_multiroom_parity_with_oracle(tracer):
+    """Interior walls with door gaps, furniture, two reflections: a small
+    multi-room building traced exactly as the oracle does."""
+    from automs_gb300 import scenes
+    tris, mat, mp, xs, ys = scenes.multiroom_scene(6_000, rooms=(2, 2), seed=3)
+    lam = scenes.WAVE_LEN_60GHZ
+    src = scenes.ula(((xs[0] + xs[1]) / 2, (ys[0] + ys[1]) / 2, 2.5), (1, 0, 0), 4, lam / 2)
+    dst = scenes.rx_grid(0.25, xs[-1] - 0.25, 20, 0.25, ys[-1] - 0.25, 20, 1.5)
+    p = dict(samples_per_launch=1, launch_x=128, launch_y=128, wave_len=lam, max_reflection=2,
+             reserve_size=100, src_bptype=2, dst_bptype=0, dst_gridsize=5, src_r=0.5e-5,
+             dst_r=0.06, src_dir=[0.0, 1.0, 0.0], dst_dir=[0.0, 0.0, 0.0])
+    c = dict(tris=tris, mat=mat, mat_prop=mp, src=src, dst=dst, params=p)
+    H, st, paths = run_gpu(tracer, c)
+    Ho, so, po = oracle.trace_channel(tris, mat, mp, src, dst, p)
+    for k in cases.STAT_KEYS + ("tasks", "overflow"):
+        assert st[k] == so[k], (k, st[k], so[k])
+    assert so["rx_paths"] > 0
+    assert np.array_equal(paths, po)
+    assert rel(H, Ho) < 1e-5
+
+
 def test_launch_pathtrace_dropin(tracer):
     c = cases.channel_case("tiny")
     p = c["params"]
