@@ -4,7 +4,8 @@
 // Replaces the OptiX GAS builds of the reference (optixPathTracer.cpp:382-546:
 // one triangle GAS, one custom-AABB GAS per sphere set) with:
 //   1. centroid bounds (one CTA reduction),
-//   2. 30-bit Morton codes with the primitive index in the low word,
+//   2. 30-bit Morton codes with the primitive index in the low word (bit 30
+//      set for primitives larger than a quarter of the scene),
 //   3. a stable LSD radix sort (one 1024-thread CTA, 4-bit digits, warp
 //      ballots for the in-tile ranks),
 //   4. the Karras hierarchy, one thread per internal node,
@@ -80,6 +81,16 @@ __global__ void k_morton(const PrimBox *boxes, int n, const float *b6, uint64_t 
     q[k] = (uint32_t)fminf(u * 1024.0f, 1023.0f);
   }
   uint32_t m = (expand10(q[0]) << 2) | (expand10(q[1]) << 1) | expand10(q[2]);
+  // Primitives larger than a quarter of the scene (floors, walls) get a bit
+  // above the Morton code, so the root splits them off into their own
+  // subtree instead of inflating the boxes of every node on the way to the
+  // small ones around their centroids.  Culling only: results do not change.
+  float bext = 0.0f, sext = 0.0f;
+  for (int k = 0; k < 3; k++) {
+    bext = fmaxf(bext, b.hi[k] - b.lo[k]);
+    sext = fmaxf(sext, b6[3 + k] - b6[k]);
+  }
+  if (sext > 0.0f && bext > 0.25f * sext) m |= 1u << 30;
   keys[i] = ((uint64_t)m << 32) | (uint32_t)i;
 }
 
