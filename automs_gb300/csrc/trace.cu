@@ -454,102 +454,280 @@ struct Slot {
 
 
 
-__global__ void __launch_bounds__(128, 7) k_stage1(TraceDev P) {
-  const long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long n_launch = (long long)P.launch_x * P.launch_y;
-  unsigned long long my_records = 0, my_segs = 0;
-  bool capped = false;
-  if (li < n_launch) {
-    const int ix = (int)(li / P.launch_y), iy = (int)(li % P.launch_y);
-    uint32_t seed = tea4((uint32_t)ix * (uint32_t)P.launch_y + (uint32_t)iy, 0u);
-    int res_cnt = 0;
-    int rec[AMS_MAX_RESERVE];  // cell * 8 + hit_cnt of the records kept so far
-    Slot slots[32];
-    const int L = P.L;
-    for (int launch = 0; launch < P.spl; launch++) {
-      float rs = rnd(seed) * (float)P.n_src;
+// Stage 1 runs as a persistent loop per warp with dynamic fetching (after
+// Aila & Laine, "Understanding the efficiency of ray traversal on GPUs",
+// HPG 2009).  All lanes visit BVH nodes of their own closest-hit queries
+// (Rx spheres, then the scene pruned at the sphere hit) in one loop whose
+// body is a single node visit, until every lane's query has ended; then all
+// lanes handle their hits together and set up their next queries (the next
+// segment, the next pending slot, the next sub-launch, or a launch index
+// fetched from a global counter), and the next round of node visits starts.
+// Lanes that finish a short ray take new work instead of idling behind the
+// warp's longest ray, and the hit code runs once per round for the whole
+// warp.  (Handling the hits of a subset of lanes while the others still
+// traverse measured slower at every threshold tried: the hit code is long.)
+// Per launch index the queries, hits and records come in the order of the
+// sequential trace (slots in increasing index, which is the order
+// __ffs(pending) gives because a spawned slot always has a higher index than
+// its parent), so the per-thread min_hc dedup and the reserve cap see
+// exactly what they see in the reference.
+enum { PH_RX = 0, PH_SCENE = 1, PH_HIT = 2 };
+
+// warp-aggregated fetch of one launch index per calling lane
+__device__ __forceinline__ long long fetch_launch(unsigned long long *ctr) {
+  const unsigned m = __activemask();
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(ctr, (unsigned long long)__popc(m));
+  base = __shfl_sync(m, base, leader);
+  return (long long)(base + (unsigned long long)__popc(m & ((1u << lane) - 1u)));
+}
+
+struct S1Query {
+  RayT r;
+  af3 Dq;  // unit direction for the sphere tests
+  Hit best;
+  int phase, node, sp;
+};
+
+// first node of the query's next instance, or PH_HIT; one-primitive
+// instances are tested here (they have no nodes)
+__device__ __forceinline__ void s1_enter(const TraceDev &P, S1Query &q, int phase) {
+  q.node = 0;
+  q.sp = 0;
+  if (phase == PH_RX) {
+    if (P.n_dst > 1) { q.phase = PH_RX; return; }
+    if (P.n_dst == 1) test_prim<2>(P.rx_prims, 0, q.r, q.best, P.dst_r, q.Dq);
+  }
+  if (P.n_tri > 1) { q.phase = PH_SCENE; return; }
+  if (P.n_tri == 1) test_prim<0>(P.tri_prims, 0, q.r, q.best, 0.0f, q.Dq);
+  q.phase = PH_HIT;
+}
+
+struct S1Ray {
+  long long li;
+  int ix, iy, launch, res_cnt;
+  uint32_t seed;
+  bool capped;
+  af3 spos;
+  unsigned pending;
+  int cur, ttl, guard;
+};
+
+// the hit of the finished query (stage-1 closest-hit program,
+// optixPathTracer.cu:285-331)
+__device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, Slot *slots,
+                                    int *rec, unsigned long long &my_records) {
+  const int L = P.L;
+  if (q.best.inst == 3) { w.ttl = 0; return; }
+  const af3 d = q.r.d;
+  const af3 o = add3(q.r.o, scl3(d, q.best.t));
+  q.r.o = o;
+  if (q.best.inst == 0 && w.ttl > 1) {
+    af3 v0, v1, v2;
+    scene_tri(P, q.best.prim, v0, v1, v2);
+    af3 N0 = nrm3(cross3(sub3(v1, v0), sub3(v2, v0)));
+    af3 N = faceforward3(N0, neg3(d), N0);
+    int m = __ldg(P.mat + q.best.prim);
+    float ct = dot3(d, N) / (len3(N) * len3(d));
+    int tid = theta_id(ct);
+    bool pen = __ldg(P.mat_prop + tid + m * AMS_NBINS) < 0.0f;
+    w.ttl--;
+    int hc = L + 1 - w.ttl;
+    int j = w.cur | (1 << (hc - 1));
+    Slot &c = slots[j];
+    c.ttl = w.ttl;
+    c.o = o;
+    c.d = sub3(d, scl3(N, 2.0f * dot3(d, N)));
+    c.M = slots[w.cur].M;
+    af3 V = sub3(v0, image_of(c.M, w.spos));
+    af3 Nimg = faceforward3(N0, V, N0);
+    image_update(c.M, Nimg, v0);
+    w.pending |= 1u << j;
+    if (!pen) w.ttl = 0;
+  } else if (q.best.inst == 2) {
+    if (w.res_cnt < P.reserve) {
+      int d0 = q.best.prim / P.n1_dst, d1 = q.best.prim % P.n1_dst;
+      int cell = (d0 / P.gs) * P.n1g + d1 / P.gs;
+      int hc = L + 1 - w.ttl;
+      int mhc = 0;
+      for (int k = w.res_cnt - 1; k >= 0; k--)
+        if ((rec[k] >> 3) == cell) { mhc = (rec[k] & 7) + 1; break; }
+      if (mhc <= hc) {
+        rec[w.res_cnt++] = cell * 8 + hc;
+        int32_t key[14];
+#pragma unroll
+        for (int k = 0; k < 12; k++) key[k] = fbits(slots[w.cur].M.m[k]);
+        key[12] = hc;
+        key[13] = w.cur;
+        int slot = path_insert(P, key);
+        if (slot >= 0) set_bit(P.T + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
+        my_records++;
+      }
+    } else {
+      w.capped = true;
+    }
+  }
+}
+
+// next query of the lane: the current slot's next segment, the next pending
+// slot, the next sub-launch, or the next launch index.  Returns false when
+// no launch index is left.
+__device__ __forceinline__ bool s1_next(const TraceDev &P, S1Query &q, S1Ray &w, Slot *slots,
+                                     long long n_launch, unsigned long long &my_capped) {
+  while (true) {
+    if (w.ttl > 0) {
+      if (++w.guard > AMS_SEG_CAP) {
+        atomicOr(P.err, AMS_DERR_LOOP);
+        w.ttl = 0;
+        continue;
+      }
+      ray_setup(q.r, q.r.o, q.r.d);
+      q.Dq = unit_dir(q.r);
+      q.best.t = AMS_TMAX; q.best.inst = 3; q.best.prim = 0x7fffffff;
+      s1_enter(P, q, PH_RX);
+      return true;
+    }
+    if (w.pending) {
+      w.cur = __ffs(w.pending) - 1;
+      w.pending &= w.pending - 1u;
+      q.r.o = slots[w.cur].o;
+      q.r.d = slots[w.cur].d;
+      w.ttl = slots[w.cur].ttl;
+      w.guard = 0;
+      continue;
+    }
+    if (w.li >= 0 && w.launch < P.spl) {
+      w.launch++;
+      float rs = rnd(w.seed) * (float)P.n_src;
       uint32_t src = (uint32_t)rs;
       if (src >= (uint32_t)P.n_src) src = (uint32_t)P.n_src - 1u;
-      const af3 spos = ld3(P.src + 3 * src);
-      slots[0].o = spos;
-      slots[0].d = rand_dir(seed, (uint32_t)ix, (uint32_t)iy, P.launch_x, P.launch_y);
+      w.spos = ld3(P.src + 3 * src);
+      slots[0].o = w.spos;
+      slots[0].d = rand_dir(w.seed, (uint32_t)w.ix, (uint32_t)w.iy, P.launch_x, P.launch_y);
 #pragma unroll
       for (int k = 0; k < 12; k++) slots[0].M.m[k] = (k == 0 || k == 5 || k == 10) ? 1.0f : 0.0f;
-      slots[0].ttl = L + 1;
-      unsigned pending = 1u;
-      while (pending) {
-        const int i = __ffs(pending) - 1;
-        pending &= pending - 1u;
-        af3 o = slots[i].o, d = slots[i].d;
-        int ttl = slots[i].ttl;
-        int guard = 0;
-        while (ttl > 0) {
-          if (++guard > AMS_SEG_CAP) { atomicOr(P.err, AMS_DERR_LOOP); break; }
-          Hit h = closest(P, o, d, 5);
-          my_segs++;
-          if (h.inst == 3) break;
-          o = add3(o, scl3(d, h.t));
-          if (h.inst == 0 && ttl > 1) {
-            af3 v0, v1, v2;
-            scene_tri(P, h.prim, v0, v1, v2);
-            af3 N0 = nrm3(cross3(sub3(v1, v0), sub3(v2, v0)));
-            af3 N = faceforward3(N0, neg3(d), N0);
-            int m = __ldg(P.mat + h.prim);
-            float ct = dot3(d, N) / (len3(N) * len3(d));
-            int tid = theta_id(ct);
-            bool pen = __ldg(P.mat_prop + tid + m * AMS_NBINS) < 0.0f;
-            ttl--;
-            int hc = L + 1 - ttl;
-            int j = i | (1 << (hc - 1));
-            Slot &c = slots[j];
-            c.ttl = ttl;
-            c.o = o;
-            c.d = sub3(d, scl3(N, 2.0f * dot3(d, N)));
-            c.M = slots[i].M;
-            af3 V = sub3(v0, image_of(c.M, spos));
-            af3 Nimg = faceforward3(N0, V, N0);
-            image_update(c.M, Nimg, v0);
-            pending |= 1u << j;
-            if (!pen) ttl = 0;
-          } else if (h.inst == 2) {
-            if (res_cnt < P.reserve) {
-              int d0 = h.prim / P.n1_dst, d1 = h.prim % P.n1_dst;
-              int cell = (d0 / P.gs) * P.n1g + d1 / P.gs;
-              int hc = L + 1 - ttl;
-              int mhc = 0;
-              for (int k = res_cnt - 1; k >= 0; k--)
-                if ((rec[k] >> 3) == cell) { mhc = (rec[k] & 7) + 1; break; }
-              if (mhc <= hc) {
-                rec[res_cnt++] = cell * 8 + hc;
-                int32_t key[14];
-#pragma unroll
-                for (int k = 0; k < 12; k++) key[k] = fbits(slots[i].M.m[k]);
-                key[12] = hc;
-                key[13] = i;
-                int slot = path_insert(P, key);
-                if (slot >= 0)
-                  set_bit(P.T + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
-                my_records++;
+      slots[0].ttl = P.L + 1;
+      w.pending = 1u;
+      continue;
+    }
+    if (w.li >= 0 && w.capped) my_capped++;
+    w.li = fetch_launch(P.ctr + 10);
+    if (w.li >= n_launch) return false;
+    w.ix = (int)(w.li / P.launch_y);
+    w.iy = (int)(w.li % P.launch_y);
+    w.seed = tea4((uint32_t)w.ix * (uint32_t)P.launch_y + (uint32_t)w.iy, 0u);
+    w.launch = 0;
+    w.res_cnt = 0;
+    w.capped = false;
+  }
+}
+
+// 8 CTAs of 128 per SM (64 registers) measured fastest among 4 to 12
+__global__ void __launch_bounds__(128, 8) k_stage1(TraceDev P) {
+  const long long n_launch = (long long)P.launch_x * P.launch_y;
+  unsigned long long my_records = 0, my_segs = 0, my_capped = 0;
+  int rec[AMS_MAX_RESERVE];  // cell * 8 + hit_cnt of the records kept so far
+  Slot slots[32];
+  int st_node[AMS_STACK];
+  float st_t[AMS_STACK];
+
+  S1Ray w;
+  w.li = -1; w.ix = 0; w.iy = 0; w.launch = 0; w.res_cnt = 0; w.seed = 0u; w.capped = false;
+  w.spos = mk3(0.f, 0.f, 0.f); w.pending = 0u; w.cur = 0; w.ttl = 0; w.guard = 0;
+  S1Query q;
+  ray_setup(q.r, mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 1.f));
+  q.Dq = mk3(0.f, 0.f, 1.f);
+  q.best.t = AMS_TMAX; q.best.inst = 3; q.best.prim = 0x7fffffff;
+  q.phase = PH_HIT; q.node = 0; q.sp = 0;
+  bool live = s1_next(P, q, w, slots, n_launch, my_capped);
+
+  while (__any_sync(0xffffffffu, live)) {
+    // ---- traversal: node visits until every lane's query has ended
+    while (true) {
+      const bool trav = live && q.phase != PH_HIT;
+      if (__ballot_sync(0xffffffffu, trav) == 0u) break;
+      if (trav) {
+        const bool rx = q.phase == PH_RX;
+        const BvhNode *nodes = rx ? P.rx_nodes : P.tri_nodes;
+        const float4 *prims = rx ? P.rx_prims : P.tri_prims;
+        const int n = rx ? P.n_dst : P.n_tri;
+        bool more = true;
+        if ((unsigned)q.node >= (unsigned)(n - 1)) {
+          atomicOr(P.err, AMS_DERR_BVH);
+          more = false;
+        } else {
+          const float4 *np = reinterpret_cast<const float4 *>(nodes + q.node);
+          const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+          const int4 d = __ldg(reinterpret_cast<const int4 *>(np + 3));
+          float tn0, tn1;
+          bool h0 = child_test(q.r, a.x, a.y, a.z, a.w, b.x, b.y, q.best.t, tn0);
+          bool h1 = child_test(q.r, b.z, b.w, c.x, c.y, c.z, c.w, q.best.t, tn1);
+          // leaves: one test site for both children
+          int lf0 = (h0 && d.x < 0) ? ~d.x : -1;
+          int lf1 = (h1 && d.y < 0) ? ~d.y : -1;
+          if (lf0 >= 0) h0 = false;
+          if (lf1 >= 0) h1 = false;
+          if (lf0 >= n || lf1 >= n) {
+            atomicOr(P.err, AMS_DERR_BVH);
+            more = false;
+          } else {
+#pragma unroll 1
+            for (int k = 0; k < 2; k++) {
+              const int lf = k == 0 ? lf0 : lf1;
+              if (lf < 0) continue;
+              if (rx) test_prim<2>(prims, lf, q.r, q.best, P.dst_r, q.Dq);
+              else test_prim<0>(prims, lf, q.r, q.best, 0.0f, q.Dq);
+            }
+            if (h0 && h1) {
+              int nearn = d.x, farn = d.y;
+              float tfar = tn1;
+              if (tn1 < tn0) { nearn = d.y; farn = d.x; tfar = tn0; }
+              if (q.sp < AMS_STACK) {
+                st_node[q.sp] = farn; st_t[q.sp] = tfar; q.sp++;
+              } else {
+                atomicOr(P.err, AMS_DERR_STACK);
               }
+              q.node = nearn;
+            } else if (h0) {
+              q.node = d.x;
+            } else if (h1) {
+              q.node = d.y;
             } else {
-              capped = true;
+              more = false;
+              const float lim = __fmaf_rn(q.best.t, 1.0001f, 1e-4f);
+              while (q.sp > 0) {
+                q.sp--;
+                if (st_t[q.sp] <= lim) { q.node = st_node[q.sp]; more = true; break; }
+              }
             }
           }
         }
+        if (!more) {
+          if (rx) s1_enter(P, q, PH_SCENE);
+          else q.phase = PH_HIT;
+        }
       }
+    }
+    // ---- hits of the waiting lanes, then their next queries
+    if (live && q.phase == PH_HIT) {
+      my_segs++;
+      s1_hit(P, q, w, slots, rec, my_records);
+      live = s1_next(P, q, w, slots, n_launch, my_capped);
     }
   }
   // block-aggregated counters
-  unsigned long long r = my_records, sg = my_segs;
+  unsigned long long rr = my_records, sg = my_segs, cp = my_capped;
   for (int off = 16; off > 0; off >>= 1) {
-    r += __shfl_xor_sync(0xffffffffu, r, off);
+    rr += __shfl_xor_sync(0xffffffffu, rr, off);
     sg += __shfl_xor_sync(0xffffffffu, sg, off);
+    cp += __shfl_xor_sync(0xffffffffu, cp, off);
   }
-  unsigned cb = __ballot_sync(0xffffffffu, capped);
   if ((threadIdx.x & 31) == 0) {
-    if (r) atomicAdd(P.ctr + 0, r);
+    if (rr) atomicAdd(P.ctr + 0, rr);
     if (sg) atomicAdd(P.ctr + 8, sg);
-    if (cb) atomicAdd(P.ctr + 1, (unsigned long long)__popc(cb));
+    if (cp) atomicAdd(P.ctr + 1, cp);
   }
 }
 
@@ -780,9 +958,29 @@ int grid_for(long long n, int block) {
 }  // namespace
 
 cudaError_t trace_stage1(const TraceDev &P, cudaStream_t st) {
+  // persistent: as many CTAs as are resident at once (lanes fetch launch
+  // indices from ctr[10], zeroed with the other counters)
   long long n = (long long)P.launch_x * P.launch_y;
-  int blocks = (int)((n + 127) / 128);
-  k_stage1<<<blocks, 128, 0, st>>>(P);
+  static int per_sm[64] = {0};
+  static int n_sm[64] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (per_sm[dev] == 0) {
+    int b = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_stage1, 128, 0);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    n_sm[dev] = sms > 0 ? sms : 1;
+    per_sm[dev] = b > 0 ? b : 1;
+  }
+  long long blocks = (long long)per_sm[dev] * n_sm[dev];
+  const long long need = (n + 127) / 128;
+  if (blocks > need) blocks = need;
+  if (blocks < 1) blocks = 1;
+  k_stage1<<<(int)blocks, 128, 0, st>>>(P);
   return cudaGetLastError();
 }
 
