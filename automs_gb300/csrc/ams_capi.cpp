@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/ams.h"
+#include "bvh_sah.h"
 #include "lbvh.h"
 #include "trace.h"
 
@@ -186,9 +187,32 @@ ams_status ams_scene_create(const float *tris, int n_tri, const int *mat, const 
     return fail(AMS_ERR_OOM);
   }
   auto t0 = std::chrono::steady_clock::now();
-  if ((e = lbvh_build_triangles(s->bvh, s->tris, n_tri, s->ws.base, s->bvh_out, st)) !=
-          cudaSuccess ||
-      (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+  if (n_tri >= AMS_SAH_MIN_TRIS) {
+    // large scene: SAH hierarchy built on the host from a copy of the
+    // triangles (traversal visits 20-40% fewer nodes than with the LBVH)
+    std::vector<float> ht(9 * (size_t)n_tri);
+    std::vector<BvhNode> hn;
+    std::vector<int> hp;
+    char msg[160] = {0};
+    if ((e = cudaMemcpyAsync(ht.data(), s->tris, sizeof(float) * 9 * (size_t)n_tri,
+                             cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+      set_err(errbuf, errlen, "reading the triangles: %s", cudaGetErrorString(e));
+      return fail(AMS_ERR_CUDA);
+    }
+    if (!sah_build_triangles(ht.data(), n_tri, hn, hp, msg, sizeof msg)) {
+      set_err(errbuf, errlen, "triangle BVH build: %s", msg);
+      return fail(AMS_ERR_INTERNAL);
+    }
+    if ((e = lbvh_from_host(s->bvh, s->tris, n_tri, hn.data(), hp.data(), s->bvh_out, st)) !=
+            cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+      set_err(errbuf, errlen, "triangle BVH upload: %s", cudaGetErrorString(e));
+      return fail(AMS_ERR_CUDA);
+    }
+  } else if ((e = lbvh_build_triangles(s->bvh, s->tris, n_tri, s->ws.base, s->bvh_out, st)) !=
+                 cudaSuccess ||
+             (e = cudaStreamSynchronize(st)) != cudaSuccess) {
     set_err(errbuf, errlen, "triangle BVH build: %s", cudaGetErrorString(e));
     return fail(AMS_ERR_CUDA);
   }

@@ -4,8 +4,9 @@
 // Replaces the OptiX GAS builds of the reference (optixPathTracer.cpp:382-546:
 // one triangle GAS, one custom-AABB GAS per sphere set) with:
 //   1. centroid bounds (one CTA reduction),
-//   2. 30-bit Morton codes with the primitive index in the low word (bit 30
-//      set for primitives larger than a quarter of the scene),
+//   2. 30-bit Morton codes of the centroids scaled to a cube, with the
+//      primitive index in the low word (bit 30 set for primitives larger
+//      than a quarter of the scene),
 //   3. a stable LSD radix sort (one 1024-thread CTA, 4-bit digits, warp
 //      ballots for the in-tile ranks),
 //   4. the Karras hierarchy, one thread per internal node,
@@ -73,10 +74,13 @@ __global__ void k_morton(const PrimBox *boxes, int n, const float *b6, uint64_t 
   if (i >= n) return;
   const PrimBox b = boxes[i];
   uint32_t q[3];
+  // one scale for all axes (the largest centroid extent): a flat room or
+  // building gets its first splits across its long sides instead of cutting
+  // its 3 m height as finely as its 45 m width
+  const float cube = fmaxf(fmaxf(b6[3] - b6[0], b6[4] - b6[1]), b6[5] - b6[2]);
   for (int k = 0; k < 3; k++) {
     float c = 0.5f * (b.lo[k] + b.hi[k]);
-    float ext = b6[3 + k] - b6[k];
-    float u = ext > 0.0f ? (c - b6[k]) / ext : 0.5f;
+    float u = cube > 0.0f ? (c - b6[k]) / cube : 0.5f;
     u = fminf(fmaxf(u, 0.0f), 1.0f);
     q[k] = (uint32_t)fminf(u * 1024.0f, 1023.0f);
   }
@@ -344,6 +348,25 @@ cudaError_t lbvh_build_spheres(Lbvh &out, const float *pos, const float *aabb, i
   cudaError_t e = build_common(out, n, scratch, outbuf, st);
   if (e != cudaSuccess || n == 0) return e;
   k_pack_spheres<<<nblk(n, 256), 256, 0, st>>>(pos, aabb, out.perm, n, out.prims);
+  return cudaGetLastError();
+}
+
+cudaError_t lbvh_from_host(Lbvh &out, const float *tris, int n, const BvhNode *h_nodes,
+                           const int *h_perm, char *outbuf, cudaStream_t st) {
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  out.n = n;
+  out.nodes = (BvhNode *)outbuf;
+  out.perm = (int *)(outbuf + al(sizeof(BvhNode) * (size_t)(n > 1 ? n - 1 : 1)));
+  out.prims = (float4 *)((char *)out.perm + al(sizeof(int) * (size_t)n));
+  if (n == 0) return cudaSuccess;
+  cudaError_t e;
+  if (n > 1 && (e = cudaMemcpyAsync(out.nodes, h_nodes, sizeof(BvhNode) * (size_t)(n - 1),
+                                    cudaMemcpyHostToDevice, st)) != cudaSuccess)
+    return e;
+  if ((e = cudaMemcpyAsync(out.perm, h_perm, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice,
+                           st)) != cudaSuccess)
+    return e;
+  k_pack_tris<<<nblk(n, 256), 256, 0, st>>>(tris, out.perm, n, out.prims);
   return cudaGetLastError();
 }
 

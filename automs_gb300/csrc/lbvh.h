@@ -23,4 +23,9 @@ cudaError_t lbvh_build_triangles(Lbvh &out, const float *tris, int n, char *scra
                                  char *outbuf, cudaStream_t st);
 cudaError_t lbvh_build_spheres(Lbvh &out, const float *pos, const float *aabb, int n,
                                char *scratch, char *outbuf, cudaStream_t st);
+// adopts a hierarchy built on the host (bvh_sah.h) for triangles already on
+// the device: copies nodes and perm into outbuf (the caller keeps the host
+// arrays alive until the stream has run) and packs the sorted triangles
+cudaError_t lbvh_from_host(Lbvh &out, const float *tris, int n, const BvhNode *h_nodes,
+                           const int *h_perm, char *outbuf, cudaStream_t st);
 cudaError_t sphere_aabbs(const float *pos, int n, float r, float *aabb, cudaStream_t st);
