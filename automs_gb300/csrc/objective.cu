@@ -819,11 +819,13 @@ __global__ void k_tc_dw_sum(const float *GU, const float *dwp, int C, int S, int
 //   dphi[k] = -sum_c Im(conj(G_U[c, k]) U[c, k]) for metasurface rows;
 //   dwp[blk][c][s] = sum over the CTA's metasurface rows of
 //     G_U[c, k] e^{-j phi'_k} conj(H_a[s, k]), warp w taking s = w, w + 32, ...
-// k_stream_dw then adds the CTAs' dwp and the H_d rows G_U[c, M + s].
+// The last CTA to finish (arrival counter) forms dL/dW: the H_d rows
+// G_U[c, M + s] plus the CTAs' dwp, a warp per entry with lanes over CTAs.
 template <int CB>
 __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int nparts,
                                                       const float *Ppart, const double *lpart,
-                                                      const float *U, float *GU, float *dwp) {
+                                                      const float *U, float *GU, float *dwp,
+                                                      unsigned *counter) {
   constexpr int NW = 32;
   const int K = M + a.S;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -917,21 +919,33 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
             make_float2(d.x, d.y);
     }
   }
-}
-
-// grad_W[c, s] = G_U[c, M + s] + sum over the tail CTAs of dwp[blk][c][s]
-__global__ void k_stream_dw(const float *GU, const float *dwp, int nblk, int C, int S, int M,
-                            float *grad_W) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= C * S) return;
-  const int c = i / S, s2 = i % S, K = M + S;
-  float2 t = reinterpret_cast<const float2 *>(GU)[(size_t)c * K + M + s2];
-  for (int b = 0; b < nblk; b++) {
-    const float2 v = reinterpret_cast<const float2 *>(dwp)[(size_t)b * C * S + i];
-    t.x += v.x;
-    t.y += v.y;
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
-  reinterpret_cast<float2 *>(grad_W)[i] = t;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int i = warp; i < a.C * a.S; i += NW) {
+    const int c = i / a.S, s2 = i % a.S;
+    c2 acc = {0.f, 0.f};
+    for (int b = lane; b < (int)gridDim.x; b += 32) {
+      const float2 v = __ldcg(reinterpret_cast<const float2 *>(dwp) + (size_t)b * a.C * a.S + i);
+      acc.x += v.x;
+      acc.y += v.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane == 0) {
+      const float2 g = __ldcg(reinterpret_cast<const float2 *>(GU) + (size_t)c * K + M + s2);
+      reinterpret_cast<float2 *>(a.grad_W)[i] = make_float2(g.x + acc.x, g.y + acc.y);
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;  // ready for the next call
 }
 
 // grad_Y = G1 + G2 / ||masked||
@@ -1364,11 +1378,13 @@ cudaError_t launch_stream_k(const ObjArgs &a, const StreamPlan &pl, const CUtens
 
 template <int CB>
 cudaError_t stream_tail(const ObjArgs &a, int M, int nparts, const float *U, const float *Pp,
-                        const double *lp, float *GU, float *dwp, cudaStream_t st);
+                        const double *lp, float *GU, float *dwp, unsigned *counter,
+                        cudaStream_t st);
 
 template <int CB>
 cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, float *Ppart,
-                       double *lpart, float *GU, float *dwp, unsigned *err, cudaStream_t st) {
+                       double *lpart, float *GU, float *dwp, unsigned *err, unsigned *counter,
+                       cudaStream_t st) {
   CUtensorMap mr, md;
   const float *Hr = M > 0 ? a.Hr : a.Hd;  // no metasurface: mapR is unused (Mbox = 0)
   if (!make_cmap(&mr, Hr, std::max(M, 1), a.R, pl.TR, pl.boxR) ||
@@ -1385,17 +1401,16 @@ cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, 
     default: e = launch_stream_k<CB, 2>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
   }
   if (e != cudaSuccess) return e;
-  return stream_tail<CB>(a, M, pl.grid, U, Ppart, lpart, GU, dwp, st);
+  return stream_tail<CB>(a, M, pl.grid, U, Ppart, lpart, GU, dwp, counter, st);
 }
 
 // after a streaming kernel: G_U, dphi and the dL/dW parts, then dL/dW
 template <int CB>
 cudaError_t stream_tail(const ObjArgs &a, int M, int nparts, const float *U, const float *Pp,
-                        const double *lp, float *GU, float *dwp, cudaStream_t st) {
+                        const double *lp, float *GU, float *dwp, unsigned *counter,
+                        cudaStream_t st) {
   const int K = M + a.S, nblk = (K + 31) / 32;
-  k_stream_tail<CB><<<nblk, 1024, 0, st>>>(a, M, nparts, Pp, lp, U, GU, dwp);
-  if (a.grad_W)
-    k_stream_dw<<<(a.C * a.S + 127) / 128, 128, 0, st>>>(GU, dwp, nblk, a.C, a.S, M, a.grad_W);
+  k_stream_tail<CB><<<nblk, 1024, 0, st>>>(a, M, nparts, Pp, lp, U, GU, dwp, counter);
   return cudaGetLastError();
 }
 
@@ -1877,8 +1892,8 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
     double *lp = reinterpret_cast<double *>(scratch + L.lp);
     unsigned *err = reinterpret_cast<unsigned *>(scratch + L.inv + 48);
     float *GUs = reinterpret_cast<float *>(scratch + L.GUs);
-    if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Um, Pp, lp, GUs, gw, err, st);
-    return run_stream<2>(a, pl, M, Um, Pp, lp, GUs, gw, err, st);
+    if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Um, Pp, lp, GUs, gw, err, counter + 2, st);
+    return run_stream<2>(a, pl, M, Um, Pp, lp, GUs, gw, err, counter + 2, st);
   }
   switch (cbucket(a.C)) {
 #define CASE(CB) case CB: return run_cb<CB>(a, sp, M, Um, Ypart, G1, G2, part, counter, scal, GUp, gw, st);
@@ -2001,7 +2016,7 @@ cudaError_t run_plan_stream(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st) {
   double *lp = reinterpret_cast<double *>(p->mem + p->oLp);
   float *gw = reinterpret_cast<float *>(p->mem + p->oGwS);
   char *ctl = p->mem + p->oCtl;
-  unsigned *counter = reinterpret_cast<unsigned *>(ctl + 36);
+  unsigned *counter = reinterpret_cast<unsigned *>(ctl + 40);
   unsigned *err = reinterpret_cast<unsigned *>(ctl + 48);
   const long long n = (long long)M * a.C * 8;
   k_prep_wide<<<(int)((n + 255) / 256), 256, 0, st>>>(a, M, U);
@@ -2012,9 +2027,8 @@ cudaError_t run_plan_stream(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st) {
     default: e = launch_stream_ht_k<CB, 2>(p, a, U, Pp, lp, err, st); break;
   }
   if (e != cudaSuccess) return e;
-  (void)counter;
   return stream_tail<CB>(a, M, p->tGrid, U, Pp, lp, gw, reinterpret_cast<float *>(p->mem + p->oDw),
-                         st);
+                         counter, st);
 }
 }  // namespace
 

@@ -16,9 +16,9 @@ struct ObjArgs {
 };
 
 // Byte offsets of the scratch regions for one problem size.  The first 256
-// bytes are a control block at a fixed offset: a float (1/||masked||) at 0 and
-// two last-CTA arrival counters (uint32) at 32 and 36, and a wait-timeout flag
-// word at 48.  They must be zero before the first call; every call leaves the
+// bytes are a control block at a fixed offset: a float (1/||masked||) at 0,
+// three last-CTA arrival counters (uint32) at 32, 36 and 40, and a
+// wait-timeout flag word at 48.  They must be zero before the first call; every call leaves the
 // counters at zero again.
 struct ObjScratchLayout {
   size_t U, G1, G2, part, GU, inv, Um, gw, Pp, lp, GUs, total;
