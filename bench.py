@@ -31,7 +31,13 @@ METRIC = "coverage Rx-paths/s"
 UNIT = "Rx-paths/s"
 WORKLOAD = ("coverage-128: 12x8x3 m room + 20 boxes (2172 tris), 16-el ULA @60 GHz, "
             "128x128 Rx at 1.5 m, 1000x1000 launch, max_reflection=2")
-FLOP_PER_SEGMENT = 520  # closest-hit query on a ~2.1k-triangle scene (ideal leaf-4 BVH)
+# Ideal-BVH work of one closest-hit query (leaf-4 tree: 2 ceil(log2 ceil(N/4))
+# slab tests of 18 flop + 4 primitive tests): 520 flop on the 2172-triangle
+# scene (40-flop triangle tests); a stage-1 query also walks the 16,384 Rx
+# spheres (24 slab tests + 4 20-flop sphere tests = 512 flop).
+FLOP_PER_SEGMENT = 520
+FLOP_PER_SEGMENT_FWD = 520 + 512
+RECORD_BYTES = 60  # one forward record of the reference (Path + grid index)
 
 
 def peaks():
@@ -119,6 +125,11 @@ def profile_value(name, key):
 def stage2_traffic():
     """DRAM bytes (read + write) of k_stage2 over one coverage-128 trace."""
     return profile_value("k_stage2_coverage128_traffic.md", "traffic_bytes_per_trace")
+
+
+def stage1_traffic():
+    """DRAM bytes (read + write) of one k_stage1 launch on coverage-128."""
+    return profile_value("k_stage1_coverage128_traffic.md", "traffic_bytes_per_launch")
 
 
 def kernel_launches(stats, aabbs_given):
@@ -702,14 +713,19 @@ def main():
     clocks = clk.summary()
     hbm, peak_kind = peaks()
     k2_ms = st0["ms_stage2_kernel"]
+    k1_ms = st0["ms_stage1"]
     succ = st0["rx_paths"]
-    alg_bytes = 32 * succ + 64 * st0["tasks"]
-    achieved = alg_bytes / (k2_ms * 1e-3) / 1e9 if k2_ms > 0 else 0.0
     sm_mhz = clocks["sm_mhz"] or 2070.0
     fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-    flops = FLOP_PER_SEGMENT * st0["segments_bwd"]
-    tflops = flops / (k2_ms * 1e-3) / 1e12 if k2_ms > 0 else 0.0
-    traffic = stage2_traffic()
+    # stage 1 (the dominant kernel): algorithmic output = the reference's
+    # forward records (60 B each); work = ideal-BVH flop per query
+    alg1 = RECORD_BYTES * st0["fwd_records"]
+    gbs1 = alg1 / (k1_ms * 1e-3) / 1e9 if k1_ms > 0 else 0.0
+    tfl1 = FLOP_PER_SEGMENT_FWD * st0["segments_fwd"] / (k1_ms * 1e-3) / 1e12 if k1_ms > 0 else 0.0
+    # stage 2: 32 B per verified backward ray + 64 B per task
+    alg2 = 32 * succ + 64 * st0["tasks"]
+    gbs2 = alg2 / (k2_ms * 1e-3) / 1e9 if k2_ms > 0 else 0.0
+    tfl2 = FLOP_PER_SEGMENT * st0["segments_bwd"] / (k2_ms * 1e-3) / 1e12 if k2_ms > 0 else 0.0
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -730,14 +746,23 @@ def main():
                    "wall_s_timed_region": t_wall, "replicas": "one seeded scene per rank"},
         "e2e": e2e,
         "gpu_launches": kernel_launches(st0, False) * args.steps,
-        "roofline": {"bound": "hbm", "kernel": "k_stage2", "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
-                     "peak_kind": peak_kind,
-                     "note": "backward traversal is ALU/latency bound; see roofline_alu"},
-        "roofline_alu": {"bound": "fp32", "kernel": "k_stage2", "achieved": tflops,
-                         "peak": fp32_peak, "unit": "TFLOP/s", "frac": tflops / fp32_peak,
-                         "flop_per_segment": FLOP_PER_SEGMENT, "segments": st0["segments_bwd"],
+        "roofline": {"bound": "hbm", "kernel": "k_stage1", "achieved": gbs1, "peak": hbm,
+                     "unit": "GB/s", "frac": gbs1 / hbm, "traffic": stage1_traffic(),
+                     "peak_kind": peak_kind, "algorithmic_bytes": alg1,
+                     "note": "forward discovery is latency/divergence bound (BVH, scene and "
+                             "path table stay in L2); see roofline_alu"},
+        "roofline_alu": {"bound": "fp32", "kernel": "k_stage1", "achieved": tfl1,
+                         "peak": fp32_peak, "unit": "TFLOP/s", "frac": tfl1 / fp32_peak,
+                         "flop_per_segment": FLOP_PER_SEGMENT_FWD,
+                         "segments": st0["segments_fwd"],
                          "peak_kind": "152 SM x 128 lanes x 2 at the sampled SM clock"},
+        "roofline_stage2": {"bound": "hbm", "kernel": "k_stage2", "achieved": gbs2, "peak": hbm,
+                            "unit": "GB/s", "frac": gbs2 / hbm, "traffic": stage2_traffic(),
+                            "peak_kind": peak_kind, "algorithmic_bytes": alg2},
+        "roofline_stage2_alu": {"bound": "fp32", "kernel": "k_stage2", "achieved": tfl2,
+                                "peak": fp32_peak, "unit": "TFLOP/s", "frac": tfl2 / fp32_peak,
+                                "flop_per_segment": FLOP_PER_SEGMENT,
+                                "segments": st0["segments_bwd"]},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "secondary": secondary,
