@@ -387,33 +387,36 @@ __device__ __forceinline__ int32_t fbits(float f) {
   return b == (int32_t)0x80000000 ? 0 : b;  // -0 and +0 are one key
 }
 
+// Path-key hashes: word-wise FNV-1a (Fowler, Noll, Vo) in 64 and 32 bits
+// with different offsets and primes, each finished by an avalanche mixer.
+// The 64-bit one places the key; the 32-bit one detects collisions.
 __device__ __forceinline__ uint64_t key_hash64(const int32_t *k) {
-  uint64_t h = 0x9E3779B97F4A7C15ull;
+  uint64_t h = 0xcbf29ce484222325ull;
 #pragma unroll
-  for (int i = 0; i < 14; i++) h = mix64(h ^ ((uint64_t)(uint32_t)k[i] + ((uint64_t)i << 40)));
-  return h;
+  for (int i = 0; i < 14; i++) h = (h ^ (uint64_t)(uint32_t)k[i]) * 0x100000001b3ull;
+  return mix64(h);
 }
 __device__ __forceinline__ uint32_t key_hash32(const int32_t *k) {
-  uint32_t h = 0x27d4eb2fu;
+  uint32_t h = 0x811c9dc5u;
 #pragma unroll
-  for (int i = 0; i < 14; i++) h = mix32(h + 0x165667b1u * (uint32_t)(k[i] ^ (i * 0x61c88647)));
-  return h;
+  for (int i = 0; i < 14; i++) h = (h ^ (uint32_t)k[i]) * 0x01000193u;
+  return mix32(h);
 }
+
+// OR a bit into a bitmap word (a reduction: the thread does not wait)
+__device__ __forceinline__ void set_bit(unsigned *word, unsigned bit) { atomicOr(word, bit); }
 
 // claim or find the slot of a path key; returns -1 when the table is full
-// OR a bit into a bitmap word unless it is already set (skips the atomic
-// for the many records of a (cell, path) pair that is already marked)
-__device__ __forceinline__ void set_bit(unsigned *word, unsigned bit) {
-  if (!(__ldcg(word) & bit)) atomicOr(word, bit);
-}
-
 __device__ int path_insert(const TraceDev &P, const int32_t *key) {
   const uint64_t h = key_hash64(key) | 1ull;
   const uint32_t c = key_hash32(key) | 1u;
   uint32_t slot = (uint32_t)h & P.tab_mask;
   for (uint32_t probe = 0; probe <= P.tab_mask; probe++) {
     // most records repeat a key already in the table: look before the CAS
+    // (both words of the slot in one round trip)
     unsigned long long old = __ldcg(P.tab_h + slot);
+    const unsigned chk = __ldcg(P.tab_chk + slot);
+    if (old == (unsigned long long)h && chk == c) return (int)slot;
     if (old == 0ull) old = atomicCAS(P.tab_h + slot, 0ull, (unsigned long long)h);
     if (old == 0ull) {
       int32_t *dst = P.tab_key + (size_t)slot * 14;
@@ -513,6 +516,10 @@ struct S1Ray {
   af3 spos;
   unsigned pending;
   int cur, ttl, guard;
+  // path-table slot of the last record's key: the key is a function of
+  // (slot, remaining levels) within one sub-launch, and consecutive records
+  // along a ray mostly repeat it
+  int key_cur, key_ttl, key_slot;
 };
 
 // the hit of the finished query (stage-1 closest-hit program,
@@ -556,12 +563,18 @@ __device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, 
         if ((rec[k] >> 3) == cell) { mhc = (rec[k] & 7) + 1; break; }
       if (mhc <= hc) {
         rec[w.res_cnt++] = cell * 8 + hc;
-        int32_t key[14];
+        int slot = w.key_slot;
+        if (w.key_cur != w.cur || w.key_ttl != w.ttl) {
+          int32_t key[14];
 #pragma unroll
-        for (int k = 0; k < 12; k++) key[k] = fbits(slots[w.cur].M.m[k]);
-        key[12] = hc;
-        key[13] = w.cur;
-        int slot = path_insert(P, key);
+          for (int k = 0; k < 12; k++) key[k] = fbits(slots[w.cur].M.m[k]);
+          key[12] = hc;
+          key[13] = w.cur;
+          slot = path_insert(P, key);
+          w.key_cur = w.cur;
+          w.key_ttl = w.ttl;
+          w.key_slot = slot;
+        }
         if (slot >= 0) set_bit(P.T + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
         my_records++;
       }
@@ -610,6 +623,7 @@ __device__ __forceinline__ bool s1_next(const TraceDev &P, S1Query &q, S1Ray &w,
       for (int k = 0; k < 12; k++) slots[0].M.m[k] = (k == 0 || k == 5 || k == 10) ? 1.0f : 0.0f;
       slots[0].ttl = P.L + 1;
       w.pending = 1u;
+      w.key_cur = -1;  // slot 0 holds a new ray: forget the last key
       continue;
     }
     if (w.li >= 0 && w.capped) my_capped++;
@@ -636,6 +650,7 @@ __global__ void __launch_bounds__(128, 8) k_stage1(TraceDev P) {
   S1Ray w;
   w.li = -1; w.ix = 0; w.iy = 0; w.launch = 0; w.res_cnt = 0; w.seed = 0u; w.capped = false;
   w.spos = mk3(0.f, 0.f, 0.f); w.pending = 0u; w.cur = 0; w.ttl = 0; w.guard = 0;
+  w.key_cur = -1; w.key_ttl = 0; w.key_slot = -1;
   S1Query q;
   ray_setup(q.r, mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 1.f));
   q.Dq = mk3(0.f, 0.f, 1.f);
