@@ -330,6 +330,7 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     P.L = p->max_reflection; P.reserve = p->reserve_size; P.spl = p->samples_per_launch;
     P.launch_x = p->launch_x; P.launch_y = p->launch_y;
     P.lam_f = (float)p->wave_len; P.lam_d = p->wave_len;
+    P.two_pi_over_lam = 6.283185307179586 / p->wave_len;
     for (int k = 0; k < 3; k++) { P.src_dir[k] = p->src_dir[k]; P.dst_dir[k] = p->dst_dir[k]; }
     P.src_bp = p->src_bptype; P.dst_bp = p->dst_bptype;
     P.tab_mask = tab_size - 1;

@@ -858,8 +858,17 @@ __global__ void __launch_bounds__(256, 4) k_stage2(TraceDev P, unsigned long lon
             if (dd > far) { fspl = lam / ((4.0f * AMS_PIF) * dres); dres = 0.0f; }
             amp *= loss * fspl;
             dres += dd;
-            float fd = (float)(2.0 * (double)max_d * (double)max_d / (double)lam);
-            far = (dd > fd) ? fd : 1e6f;
+            // far_dist = 2 max_d^2 / lambda, divided in double and rounded to
+            // float (optixPathTracer.cu:385-389).  Its value matters only when
+            // the segment is longer; a float estimate (relative error < 3e-7)
+            // with a 1e-5 margin settles the common near-field case without
+            // the double division (FP64 is slow on this part).
+            float far_next = 1e6f;
+            if (dd > ((2.0f * max_d) * max_d / lam) * 0.99999f) {
+              const float fd = (float)(2.0 * (double)max_d * (double)max_d / (double)lam);
+              far_next = (dd > fd) ? fd : 1e6f;
+            }
+            far = far_next;
             dd = 0.0f;
             if (is_ref) d = sub3(d, scl3(N, 2.0f * dot3(d, N)));
           } else if (h.inst == 1 && h.prim == s) {
@@ -873,9 +882,10 @@ __global__ void __launch_bounds__(256, 4) k_stage2(TraceDev P, unsigned long lon
           }
         }
         if (ok) {
-          // FP64 path length -> phase, reduced mod 2 pi in FP64
-          double ph = 6.283185307179586 * D / P.lam_d;
-          ph = ph - 6.283185307179586 * floor(ph / 6.283185307179586);
+          // FP64 path length -> phase, reduced mod 2 pi in FP64 (products with
+          // precomputed 2 pi / lambda and 1 / (2 pi): no FP64 division per ray)
+          double ph = D * P.two_pi_over_lam;
+          ph = ph - 6.283185307179586 * floor(ph * 0.15915494309189535);
           float sn, cs;
           sincosf((float)ph, &sn, &cs);
           double re = (double)(amp * cs), im = (double)(-amp * sn);

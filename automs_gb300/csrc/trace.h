@@ -40,6 +40,7 @@ struct TraceDev {
   int L, reserve, spl, launch_x, launch_y;
   float lam_f;
   double lam_d;
+  double two_pi_over_lam;  // 2 pi / lam_d
   float src_dir[3], dst_dir[3];
   int src_bp, dst_bp;
   // path table (open addressing, slot = path id)
