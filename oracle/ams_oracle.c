@@ -550,7 +550,8 @@ static void forward_thread(const scene_t *S, const orc_params *p, int n1_dst,
 /* backward verification of one (path, src, dst), optixPathTracer.cu:223-271
  * and :332-417.  Returns 1 on success with the complex contribution. */
 static int backward_ray(const scene_t *S, const orc_params *p, const mat34 *M,
-                        int hc, int mask, int src, int dst, double *re, double *im) {
+                        int hc, int mask, int src, int dst, double *re, double *im,
+                        int *farfield) {
   f3 o = ld3(S->dst + 3 * dst);
   f3 dir = nrm3(sub(image_of(M, ld3(S->src + 3 * src)), o));
   f3 dstdir = ld3(p->dst_dir), srcdir = ld3(p->src_dir);
@@ -582,7 +583,11 @@ static int backward_ray(const scene_t *S, const orc_params *p, const mat34 *M,
       int is_ref = (mask >> (hcb - 1)) & 1;
       float max_d = fmaxf(fmaxf(len3(sub(v0, v1)), len3(sub(v1, v2))), len3(sub(v2, v0)));
       float fspl = 1.0f;
-      if (dd > far) { fspl = lam / ((4.0f * ORC_PIF) * dres); dres = 0.0f; }
+      if (dd > far) {
+        fspl = lam / ((4.0f * ORC_PIF) * dres);
+        dres = 0.0f;
+        *farfield = 1;
+      }
       amp *= loss * fspl;
       dres += dd;
       float fd = (float)(2.0 * (double)max_d * (double)max_d / (double)lam);
@@ -773,12 +778,12 @@ int orc_trace_channel(const float *tris, int n_tri, const int *mat,
   free(recs);
 
   double *acc = (double *)calloc((size_t)n_src * n_dst * 2, sizeof(double));
-  uint64_t okc = 0, failc = 0;
+  uint64_t okc = 0, failc = 0, ffc = 0;
   for (int round = 1;; round++) {
     unsigned char *succ = (unsigned char *)calloc(nt ? nt : 1, 1);
     st->rounds++;
     st->tasks += nt;
-#pragma omp parallel for schedule(dynamic, 1) reduction(+ : okc, failc)
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : okc, failc, ffc)
     for (long ti = 0; ti < (long)nt; ti++) {
       int cell = tasks[ti].cell, pid = tasks[ti].pid;
       int gi = cell / n1g, gj = cell % n1g;
@@ -790,7 +795,9 @@ int orc_trace_channel(const float *tris, int n_tri, const int *mat,
           int d = di * n1_dst + dj;
           if (d >= n_dst) continue;
           double re, im;
-          if (backward_ray(&S, p, &pM[pid], hc, mask, s, d, &re, &im)) {
+          int ff = 0;
+          if (backward_ray(&S, p, &pM[pid], hc, mask, s, d, &re, &im, &ff)) {
+            ffc += (uint64_t)ff;
             size_t o = ((size_t)s * n_dst + d) * 2;
 #pragma omp atomic
             acc[o] += re;
@@ -826,6 +833,7 @@ int orc_trace_channel(const float *tris, int n_tri, const int *mat,
   }
   st->rx_paths = okc;
   st->rx_fail = failc;
+  st->farfield = ffc;
   for (size_t i = 0; i < (size_t)n_src * n_dst * 2; i++) result[i] += (float)acc[i];
   free(acc);
   free(tasks);

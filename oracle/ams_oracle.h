@@ -53,6 +53,8 @@ typedef struct {
   uint64_t rounds;          /* stage-2 rounds that ran */
   uint64_t tasks;           /* (path, cell) tasks traced over all rounds */
   uint64_t overflow;        /* threads that hit the reserve cap */
+  uint64_t farfield;        /* verified rays whose loss used the far-field switch
+                               (optixPathTracer.cu:369-377) at least once */
 } orc_stats;
 
 /* Full build_channel: accumulates into result[n_src*n_dst*2] (re, im).

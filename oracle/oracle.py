@@ -29,7 +29,7 @@ class OrcParams(C.Structure):
 class OrcStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "rx_paths", "rx_fail", "fwd_records", "unique_records", "unique_paths",
-        "rounds", "tasks", "overflow")]
+        "rounds", "tasks", "overflow", "farfield")]
 
 
 _lib = None

@@ -15,7 +15,8 @@ from automs_gb300 import scenes  # noqa: E402
 STAT_KEYS = ("rx_paths", "rx_fail", "fwd_records", "unique_records", "unique_paths", "rounds")
 
 CHANNEL_CASES = ("tiny", "small", "pen_l3", "allpen_l4", "ms_to_rx", "ap_to_ms",
-                 "bp3_door", "spl2_cap", "l0", "l5", "ms3_ap_rx", "ms3_ap_ms", "ms3_ms_rx")
+                 "bp3_door", "spl2_cap", "l0", "l5", "ms3_ap_rx", "ms3_ap_ms", "ms3_ms_rx",
+                 "farfield")
 
 # the three traces of the small one-metasurface channel set
 _MS3 = {"ms3_ap_rx": "src_to_dst", "ms3_ap_ms": "src_to_ms{0}", "ms3_ms_rx": "ms{0}_to_dst"}
@@ -43,7 +44,8 @@ def channel_case(name):
             tris, mat, mp = scenes.with_blackholes(tris, mat, mp, [m["blackhole"]])
         return dict(tris=tris, mat=mat, mat_prop=mp, src=t["src"], dst=t["dst"],
                     params=dict(t["params"]))
-    if name in ("tiny", "pen_l3", "allpen_l4", "ms_to_rx", "bp3_door", "spl2_cap", "l0", "l5"):
+    if name in ("tiny", "pen_l3", "allpen_l4", "ms_to_rx", "bp3_door", "spl2_cap", "l0", "l5",
+                "farfield"):
         c = scenes.coverage_config("coverage-tiny")
     elif name in ("small", "ap_to_ms"):
         c = scenes.coverage_config("coverage-small")
@@ -78,6 +80,13 @@ def channel_case(name):
         p["reserve_size"] = 3
     elif name == "l0":
         p["max_reflection"] = 0
+    elif name == "farfield":
+        # A 20 m wavelength puts second reflections in the far field of the
+        # first reflecting triangle (segment > 2 maxedge^2 / lambda,
+        # optixPathTracer.cu:369-389), which 60 GHz never does on this mesh
+        # of metre-sized triangles: the FSPL then splits at that hit.
+        p["wave_len"] = 20.0
+        p["max_reflection"] = 3
     elif name == "l5":
         c["mat_prop"][3:] *= -1
         p["max_reflection"] = 5

@@ -113,6 +113,20 @@ def test_channel_matches_reference(name):
     assert np.linalg.norm(H - Hr) / np.linalg.norm(Hr) < 2e-3
 
 
+def test_farfield_case_exercises_the_switch():
+    """The far-field FSPL split (optixPathTracer.cu:369-389) changes the loss
+    of a path only when a segment outruns 2 maxedge^2 / lambda of the
+    triangle before it; the other cases never reach it, this one must."""
+    c = cases.channel_case("farfield")
+    _, st, _ = oracle.trace_channel(c["tris"], c["mat"], c["mat_prop"], c["src"], c["dst"],
+                                    c["params"], nthreads=2)
+    assert st["farfield"] > 0.02 * st["rx_paths"]
+    t = cases.channel_case("pen_l3")
+    _, st0, _ = oracle.trace_channel(t["tris"], t["mat"], t["mat_prop"], t["src"], t["dst"],
+                                     t["params"], nthreads=2)
+    assert st0["farfield"] == 0
+
+
 @pytest.mark.parametrize("name", cases.OBJECTIVE_CASES)
 def test_objective_matches_reference_model(name):
     g = load(f"obj_{name}.npz")
