@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -155,17 +156,30 @@ ams_status ams_scene_create(const float *tris, int n_tri, const int *mat, const 
     set_err(errbuf, errlen, "scene allocation: %s", cudaGetErrorString(e));
     return fail(AMS_ERR_OOM);
   }
+  // host copy of the triangles: validated here, and the input of the SAH
+  // builder for large scenes
+  std::vector<float> ht(9 * (size_t)n_tri);
   if (n_tri > 0) {
-    // material ids index mat_prop rows: check them on the host once
+    // material ids index mat_prop rows, vertices must be finite: check on
+    // the host once (the reference accepts both and fails silently)
+    // (on the caller's stream, after whatever produced the arrays there)
     std::vector<int> hm((size_t)n_tri);
-    if ((e = cudaMemcpy(hm.data(), mat, sizeof(int) * (size_t)n_tri, cudaMemcpyDeviceToHost)) !=
-        cudaSuccess) {
-      set_err(errbuf, errlen, "reading mat: %s", cudaGetErrorString(e));
+    if ((e = cudaMemcpyAsync(hm.data(), mat, sizeof(int) * (size_t)n_tri, cudaMemcpyDeviceToHost,
+                             st)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(ht.data(), tris, sizeof(float) * 9 * (size_t)n_tri,
+                             cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
+      set_err(errbuf, errlen, "reading the scene arrays: %s", cudaGetErrorString(e));
       return fail(AMS_ERR_CUDA);
     }
     for (int i = 0; i < n_tri; i++)
       if (hm[i] < 0 || hm[i] >= n_mat) {
         set_err(errbuf, errlen, "mat[%d] = %d is outside [0, %d)", i, hm[i], n_mat);
+        return fail(AMS_ERR_ARG);
+      }
+    for (size_t i = 0; i < ht.size(); i++)
+      if (!std::isfinite(ht[i])) {
+        set_err(errbuf, errlen, "triangle %zu has a non-finite vertex coordinate", i / 9);
         return fail(AMS_ERR_ARG);
       }
     if ((e = cudaMemcpyAsync(s->tris, tris, sizeof(float) * 9 * (size_t)n_tri,
@@ -188,18 +202,11 @@ ams_status ams_scene_create(const float *tris, int n_tri, const int *mat, const 
   }
   auto t0 = std::chrono::steady_clock::now();
   if (n_tri >= AMS_SAH_MIN_TRIS) {
-    // large scene: SAH hierarchy built on the host from a copy of the
+    // large scene: SAH hierarchy built on the host from the host copy of the
     // triangles (traversal visits 20-40% fewer nodes than with the LBVH)
-    std::vector<float> ht(9 * (size_t)n_tri);
     std::vector<BvhNode> hn;
     std::vector<int> hp;
     char msg[160] = {0};
-    if ((e = cudaMemcpyAsync(ht.data(), s->tris, sizeof(float) * 9 * (size_t)n_tri,
-                             cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(st)) != cudaSuccess) {
-      set_err(errbuf, errlen, "reading the triangles: %s", cudaGetErrorString(e));
-      return fail(AMS_ERR_CUDA);
-    }
     if (!sah_build_triangles(ht.data(), n_tri, hn, hp, msg, sizeof msg)) {
       set_err(errbuf, errlen, "triangle BVH build: %s", msg);
       return fail(AMS_ERR_INTERNAL);
@@ -903,11 +910,14 @@ ams_status ams_mlp_train_step(ams_mlp *m, const float *X, const float *T, int B,
   return mlp_check_err(m, st, errbuf, errlen);
 }
 
-static void mlp_param_copy(MlpDev &d, float *flat, bool to_flat, bool grads, cudaStream_t st) {
+// which: 0 parameters, 1 gradients, 2 Adam first moments, 3 second moments
+static void mlp_param_copy(MlpDev &d, float *flat, bool to_flat, int which, cudaStream_t st) {
   size_t o = 0;
   for (int l = 1; l <= d.L; l++) {
-    float *W = grads ? d.gW[l] : d.W[l];
-    float *b = grads ? d.gb[l] : d.b[l];
+    float *const Ws[4] = {d.W[l], d.gW[l], d.mW[l], d.vW[l]};
+    float *const bs[4] = {d.b[l], d.gb[l], d.mb[l], d.vb[l]};
+    float *W = Ws[which];
+    float *b = bs[which];
     const size_t dp = sizeof(float) * d.dp[l - 1], dl = sizeof(float) * d.d[l - 1];
     if (to_flat)
       cudaMemcpy2DAsync(flat + o, dl, W, dp, dl, d.d[l], cudaMemcpyDeviceToDevice, st);
@@ -932,7 +942,7 @@ ams_status ams_mlp_gradients(ams_mlp *m, const float *X, const float *T, int B, 
   cudaStream_t st = (cudaStream_t)stream;
   CK(mlp_forward(m->dev, X, B, nullptr, st));
   CK(mlp_backward(m->dev, T, B, loss, st));
-  mlp_param_copy(m->dev, grads, true, true, st);
+  mlp_param_copy(m->dev, grads, true, 1, st);
   CK(cudaGetLastError());
   return mlp_check_err(m, st, errbuf, errlen);
 }
@@ -948,8 +958,29 @@ ams_status ams_mlp_params(ams_mlp *m, float *params, int direction, long long *c
   if (count) *count = n;
   if (!params) return AMS_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  mlp_param_copy(m->dev, params, direction == 0, false, st);
+  mlp_param_copy(m->dev, params, direction == 0, 0, st);
   if (direction == 1) CK(mlp_refresh_bf16(m->dev, st));
+  CK(cudaStreamSynchronize(st));
+  return AMS_OK;
+}
+
+ams_status ams_mlp_adam_state(ams_mlp *m, float *m1, float *m2, long long *step, int direction,
+                              void *stream, char *errbuf, size_t errlen) {
+  clear_stale_error();
+  if (!m || !m1 || !m2 || !step || (direction != 0 && direction != 1)) {
+    set_err(errbuf, errlen, "bad arguments");
+    return AMS_ERR_ARG;
+  }
+  if (direction == 1 && (*step < 0 || *step > 0x7fffffffLL)) {
+    set_err(errbuf, errlen, "Adam step %lld out of range", *step);
+    return AMS_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  mlp_param_copy(m->dev, m1, direction == 0, 2, st);
+  mlp_param_copy(m->dev, m2, direction == 0, 3, st);
+  CK(cudaGetLastError());
+  if (direction == 0) *step = m->dev.step;
+  else m->dev.step = (int)*step;
   CK(cudaStreamSynchronize(st));
   return AMS_OK;
 }

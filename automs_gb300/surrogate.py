@@ -106,6 +106,37 @@ class MLP:
             raise ValueError("parameter count mismatch")
         call("ams_mlp_params", self._h, _ptr(p), 1, None, _stream())
 
+    def state_dict(self):
+        """Everything needed to resume training: widths, FP32 parameters,
+        Adam moments and step (CPU tensors)."""
+        m1 = torch.empty(self.n_params, device="cuda")
+        m2 = torch.empty(self.n_params, device="cuda")
+        step = C.c_longlong(0)
+        call("ams_mlp_adam_state", self._h, _ptr(m1), _ptr(m2), C.byref(step), 0, _stream())
+        return {"dims": list(self.dims), "params": self.get_params().cpu(), "adam_m": m1.cpu(),
+                "adam_v": m2.cpu(), "adam_step": int(step.value)}
+
+    def load_state_dict(self, sd):
+        if list(sd["dims"]) != self.dims:
+            raise ValueError(f"checkpoint widths {sd['dims']} != {self.dims}")
+        self.set_params(sd["params"])
+        m1 = sd["adam_m"].to(device="cuda", dtype=torch.float32).contiguous()
+        m2 = sd["adam_v"].to(device="cuda", dtype=torch.float32).contiguous()
+        if m1.numel() != self.n_params or m2.numel() != self.n_params:
+            raise ValueError("Adam state size mismatch")
+        step = C.c_longlong(int(sd["adam_step"]))
+        call("ams_mlp_adam_state", self._h, _ptr(m1), _ptr(m2), C.byref(step), 1, _stream())
+
+    def save(self, path):
+        torch.save(self.state_dict(), path)
+
+    @classmethod
+    def load(cls, path, max_batch=4096):
+        sd = torch.load(path, map_location="cpu")
+        net = cls(sd["dims"], max_batch=max_batch)
+        net.load_state_dict(sd)
+        return net
+
     def fit(self, X, T, epochs=10, batch=1024, lr=1e-3, seed=0, lr_decay=1.0):
         """Minibatch Adam over (X, T); returns the per-epoch mean losses."""
         g = torch.Generator(device="cpu").manual_seed(seed)

@@ -255,6 +255,16 @@ ams_status ams_mlp_gradients(ams_mlp *mlp, const float *X, const float *T,
 ams_status ams_mlp_params(ams_mlp *mlp, float *params, int direction,
                           long long *count, void *stream, char *errbuf,
                           size_t errlen);
+/* Adam state for checkpoint / resume: first and second moments (device
+ * float arrays of ams_mlp_params' count, same layout) and the step count.
+ * direction 0 copies out, 1 copies in; with the parameters restored too,
+ * training continues exactly as if it had not stopped.  The reference keeps
+ * no learned state (its checkpoints are torch.save of results,
+ * physical_exp_nni_model.py:152-161, and the best-loss snapshot of
+ * optimize_model, go.py:320-335); this serves the surrogate. */
+ams_status ams_mlp_adam_state(ams_mlp *mlp, float *m1, float *m2,
+                              long long *step, int direction, void *stream,
+                              char *errbuf, size_t errlen);
 
 /* Device bytes held by the library's internal scratch (all objective calls
  * on this device) -- for leak checks. */

@@ -66,3 +66,29 @@ def test_mlp_params_roundtrip_and_training(S):
     hist = net.fit(X.cuda(), T.cuda(), epochs=80, batch=256, lr=3e-3)
     assert hist[-1] < 0.25 * hist[0], hist
     net.close()
+
+
+def test_checkpoint_resume_is_exact(S, tmp_path):
+    """Parameters + Adam moments + step restored into a fresh network: the
+    next steps equal those of the network that never stopped."""
+    dims = [16, 128, 128]
+    g = torch.Generator(device="cpu").manual_seed(3)
+    X = torch.randn(512, 16, generator=g).cuda()
+    T = torch.tanh(X @ torch.randn(16, 128, generator=g).cuda())
+    a = S.MLP(dims, max_batch=512, seed=5)
+    for _ in range(5):
+        a.train_step(X, T, 2e-3)
+    path = str(tmp_path / "mlp.pt")
+    a.save(path)
+    for _ in range(5):
+        a.train_step(X, T, 2e-3)
+    b = S.MLP.load(path, max_batch=512)
+    assert b.state_dict()["adam_step"] == 5
+    for _ in range(5):
+        b.train_step(X, T, 2e-3)
+    assert torch.equal(a.get_params(), b.get_params())
+    sa, sb = a.state_dict(), b.state_dict()
+    assert torch.equal(sa["adam_m"], sb["adam_m"]) and torch.equal(sa["adam_v"], sb["adam_v"])
+    assert sa["adam_step"] == sb["adam_step"] == 10
+    a.close()
+    b.close()

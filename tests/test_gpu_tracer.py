@@ -173,3 +173,18 @@ def test_errors_raise(tracer):
     _, st = sc.trace(c["src"], c["dst"], c["params"])
     assert st["rx_paths"] > 0
     sc.close()
+
+
+def test_non_finite_vertices_rejected(tracer):
+    from automs_gb300._lib import AmsError
+    c = cases.channel_case("tiny")
+    for bad in (np.nan, np.inf):
+        tris = c["tris"].copy()
+        tris.reshape(-1, 9)[7, 4] = bad
+        with pytest.raises(AmsError, match="non-finite"):
+            tracer.Scene(tris, c["mat"], c["mat_prop"])
+    # a valid scene right after works
+    sc = tracer.Scene(c["tris"], c["mat"], c["mat_prop"])
+    _, st = sc.trace(c["src"], c["dst"], c["params"])
+    assert st["rx_paths"] > 0
+    sc.close()
