@@ -32,3 +32,31 @@ def test_channel_ms_config_sizes():
     assert c["tris"].shape[0] == 50_028
     assert c["ms"].shape == (32, 32, 3) and c["dst"].shape == (256, 256, 3)
     assert set(c["traces"]) == {"src_to_dst", "src_to_ms{0}", "ms{0}_to_dst"}
+
+
+def _stl_bytes(tris, count=None):
+    import struct
+    tris = np.asarray(tris, np.float32).reshape(-1, 3, 3)
+    out = bytearray(b"synthetic".ljust(80, b" "))
+    out += struct.pack("<I", len(tris) if count is None else count)
+    for t in tris:
+        out += struct.pack("<3f", 0.0, 0.0, 1.0) + t.tobytes() + struct.pack("<H", 0)
+    return bytes(out)
+
+
+def test_read_stl_valid_and_corrupted(tmp_path):
+    import pytest
+    rng = np.random.Generator(np.random.PCG64(0))
+    tris = rng.uniform(-1, 1, size=(5, 3, 3)).astype(np.float32)
+    p = tmp_path / "ok.stl"
+    p.write_bytes(_stl_bytes(tris))
+    assert np.array_equal(scenes.read_stl(str(p)), tris)
+    p.write_bytes(_stl_bytes(np.zeros((0, 3, 3))))
+    assert scenes.read_stl(str(p)).shape == (0, 3, 3)
+    for name, data in (("empty", b""), ("short_header", b"x" * 50),
+                       ("truncated", _stl_bytes(tris)[:-7]),
+                       ("count_mismatch", _stl_bytes(tris, count=9))):
+        q = tmp_path / f"{name}.stl"
+        q.write_bytes(data)
+        with pytest.raises(ValueError):
+            scenes.read_stl(str(q))
