@@ -175,7 +175,7 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def objective_bench(torch, steps, flush):
+def objective_bench(torch, steps, flush, cpu_baseline=False):
     """Plain objective fwd+bwd, S=16 M=1024 R=4096 C=1, through the C ABI.
 
     Eight independent channel sets (274 MB, more than L2) are evaluated in
@@ -257,6 +257,26 @@ def objective_bench(torch, steps, flush):
     rel = float(((loss_plan - loss).abs() / loss.abs()).max())
     for h in plans:
         L.ams_objective_plan_destroy(h)
+    cpu = None
+    if cpu_baseline:
+        # the reference's method (PyTorch complex64 + autograd, go.py:107-245)
+        # on the host cores, same shapes, 20 evaluations
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import objective_oracle as OO
+        threads = os.cpu_count() or 1
+        torch.set_num_threads(threads)
+        Hd, Ha, Hr = (x.cpu() for x in sets[0])
+        phc, Wc = phi.cpu(), W.cpu()
+        for _ in range(3):
+            OO.torch_objective_step(torch, Hd, Ha, Hr, phc, Wc, 1.0 / R)
+        n_cpu = 20
+        t0 = time.perf_counter()
+        for _ in range(n_cpu):
+            OO.torch_objective_step(torch, Hd, Ha, Hr, phc, Wc, 1.0 / R)
+        cpu = {"value": n_cpu / (time.perf_counter() - t0), "unit": "evals/s", "cores": threads,
+               "kind": "port",
+               "sample": "20 evaluations, the reference's method (PyTorch complex64 + autograd) "
+                         "on the host CPU, same S/M/R"}
     bytes_alg = 8 * (R * M + M * S + R * S)
     hbm, kind = peaks()
     achieved = bytes_alg / (t * 1e-3) / 1e9
@@ -268,6 +288,7 @@ def objective_bench(torch, steps, flush):
                        "plan_create_ms": t_plan * 1e3},
             "direct_call": {"value": 1e3 / t_direct, "ms_per_eval": t_direct,
                             "max_rel_loss_diff": rel},
+            "cpu_baseline": cpu,
             "roofline": {"bound": "hbm", "kernel": "k_obj_stream_t", "achieved": achieved,
                          "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": profile_value("k_obj_stream_c1_traffic.md",
@@ -697,7 +718,7 @@ def main():
            "d2h_bytes_per_step": d2h,
            "note": "Scene creation (copies + triangle BVH) + trace + result download per step"}
 
-    obj = objective_bench(torch, 200, flush)
+    obj = objective_bench(torch, 200, flush, cpu_baseline=not args.no_cpu_baseline and world == 1)
     secondary = [obj]
     if not args.no_secondary:
         secondary.append(objective_codes_bench(torch, R=4096))

@@ -129,3 +129,22 @@ def mean_capacity(H_d, H_a, H_r, phi, wvec):
     loss, gW, gphi = objective_from_weights(H_d, H_a, H_r, phi, np.asarray(wvec)[None, :],
                                             1.0 / R, np.zeros(1, bool))
     return loss, gW[0], gphi
+
+
+def torch_objective_step(torch, H_d, H_a, H_r, phi, W, w, max_phase=2 * np.pi):
+    """One forward + backward of the reference's own method: PyTorch complex64
+    tensors and autograd (go.py:107-157 get_channel with one metasurface hop,
+    go.py:159-245 forward in "capacity" mode, no dropout), on whatever device
+    the tensors live.  Used as the timed CPU baseline of the objective.
+    Returns (loss, dL/dW, dL/dphi)."""
+    W = W.detach().clone().requires_grad_(True)
+    phi = phi.detach().clone().requires_grad_(True)
+    p = torch.remainder(phi, max_phase)
+    H = H_d + (H_a * torch.exp(1j * p.to(H_a.dtype))[None, :]) @ H_r
+    Y = W @ H
+    cap = torch.log2(1.0 + (Y.abs() + EPS32) ** 2 / N0)
+    mx, _ = cap.max(0)
+    masked = cap * (cap != mx[None, :])
+    loss = -w * mx.sum() + torch.linalg.norm(masked)
+    loss.backward()
+    return loss.detach(), W.grad, phi.grad

@@ -185,3 +185,23 @@ def test_objective_adjoint_finite_differences():
         fd = (OO.objective(*args, phi, t1, A, 0.5, drop)[0]
               - OO.objective(*args, phi, t2, A, 0.5, drop)[0]) / (2 * h)
         assert abs(fd - gth[i, j]) <= 1e-4 * max(1.0, abs(gth[i, j]))
+
+
+def test_torch_objective_baseline_matches_oracle():
+    """The timed CPU baseline of the objective (the reference's method:
+    PyTorch complex64 + autograd) agrees with the FP64 restatement."""
+    import torch
+    rng = np.random.Generator(np.random.PCG64(5))
+    S, M, R, Cn = 8, 64, 200, 4
+
+    def cn(*sh):
+        return ((rng.normal(size=sh) + 1j * rng.normal(size=sh)) * 1e-4).astype(np.complex64)
+    Hd, Ha, Hr = cn(S, R), cn(S, M), cn(M, R)
+    phi = rng.uniform(0, 2 * np.pi, M).astype(np.float32)
+    W = (cn(Cn, S) * 1e4).astype(np.complex64)
+    lo, gWo, gpo = OO.objective_from_weights(Hd, Ha, Hr, phi, W, 0.5, np.zeros(Cn, bool))
+    t = torch.as_tensor
+    loss, gW, gp = OO.torch_objective_step(torch, t(Hd), t(Ha), t(Hr), t(phi), t(W), 0.5)
+    assert abs(float(loss) - lo) <= 1e-4 * abs(lo)
+    assert np.abs(gW.numpy() - gWo).max() <= 1e-3 * np.abs(gWo).max()
+    assert np.abs(gp.numpy() - gpo).max() <= 1e-3 * np.abs(gpo).max()
