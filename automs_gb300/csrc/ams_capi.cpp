@@ -15,6 +15,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -33,16 +35,101 @@ void set_err(char *buf, size_t len, const char *fmt, ...) {
   va_end(ap);
 }
 
+// Device blocks of destroyed scenes kept for the next scene on the device.
+// cudaFree synchronises the whole device and cudaMalloc costs tens of
+// microseconds; a caller that builds a scene per channel (as build_channel,
+// go.py:679-767, does) would pay both on every call.  Blocks are kept in
+// power-of-two size classes per device.  A scene hands its blocks back only
+// when it is destroyed, after its last call returned (every scene call
+// synchronises its stream), so no GPU work still uses them.  On an
+// allocation failure the device's cached blocks are released and the
+// allocation retried once.
+struct BlockPool {
+  std::mutex mu;
+  std::multimap<std::pair<int, size_t>, void *> free_blocks;
+  std::vector<void *> free_pinned;  // HostCounters blocks (pinned host memory)
+};
+BlockPool &block_pool() {
+  static BlockPool *p = new BlockPool();  // lives until the process exits
+  return *p;
+}
+size_t size_class(size_t bytes) {
+  size_t c = 4096;
+  while (c < bytes) c <<= 1;
+  return c;
+}
+cudaError_t pool_malloc(void **out, size_t bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const size_t c = size_class(bytes);
+  BlockPool &bp = block_pool();
+  {
+    std::lock_guard<std::mutex> lk(bp.mu);
+    auto it = bp.free_blocks.find({dev, c});
+    if (it != bp.free_blocks.end()) {
+      *out = it->second;
+      bp.free_blocks.erase(it);
+      return cudaSuccess;
+    }
+  }
+  e = cudaMalloc(out, c);
+  if (e == cudaErrorMemoryAllocation) {
+    (void)cudaGetLastError();
+    std::vector<void *> rel;
+    {
+      std::lock_guard<std::mutex> lk(bp.mu);
+      for (auto it = bp.free_blocks.begin(); it != bp.free_blocks.end();) {
+        if (it->first.first == dev) { rel.push_back(it->second); it = bp.free_blocks.erase(it); }
+        else ++it;
+      }
+    }
+    for (void *q : rel) cudaFree(q);
+    e = cudaMalloc(out, c);
+  }
+  if (e != cudaSuccess) *out = nullptr;
+  return e;
+}
+void pool_free(void *ptr, size_t bytes, int dev) {
+  if (!ptr) return;
+  BlockPool &bp = block_pool();
+  std::lock_guard<std::mutex> lk(bp.mu);
+  bp.free_blocks.insert({{dev, size_class(bytes)}, ptr});
+}
+
+template <class T>
+cudaError_t pool_malloc_pinned(T **out) {
+  BlockPool &bp = block_pool();
+  {
+    std::lock_guard<std::mutex> lk(bp.mu);
+    if (!bp.free_pinned.empty()) {
+      *out = static_cast<T *>(bp.free_pinned.back());
+      bp.free_pinned.pop_back();
+      return cudaSuccess;
+    }
+  }
+  return cudaMallocHost(reinterpret_cast<void **>(out), sizeof(T));
+}
+void pool_free_pinned(void *ptr) {
+  if (!ptr) return;
+  BlockPool &bp = block_pool();
+  std::lock_guard<std::mutex> lk(bp.mu);
+  bp.free_pinned.push_back(ptr);
+}
+
 struct Arena {
   char *base = nullptr;
   size_t cap = 0, used = 0, high = 0;
-  ~Arena() { if (base) cudaFree(base); }
+  int dev = 0;
+  ~Arena() { pool_free(base, cap, dev); }
   cudaError_t ensure(size_t bytes) {
     if (bytes <= cap) return cudaSuccess;
-    if (base) { cudaFree(base); base = nullptr; cap = 0; }
-    cudaError_t e = cudaMalloc(&base, bytes);
+    if (base) { pool_free(base, cap, dev); base = nullptr; cap = 0; }
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = pool_malloc(reinterpret_cast<void **>(&base), bytes);
     if (e != cudaSuccess) { base = nullptr; return e; }
-    cap = bytes;
+    cap = size_class(bytes);
     high = std::max(high, bytes);
     return cudaSuccess;
   }
@@ -80,14 +167,15 @@ struct ams_scene {
   bool have_last = false;
   float ms_bvh_scene = 0.f;
   cudaEvent_t k2[2] = {nullptr, nullptr};
+  size_t tris_bytes = 0, mat_bytes = 0, mat_prop_bytes = 0, bvh_bytes = 0;
   ~ams_scene() {
     for (auto &e : k2)
       if (e) cudaEventDestroy(e);
-    if (tris) cudaFree(tris);
-    if (mat) cudaFree(mat);
-    if (mat_prop) cudaFree(mat_prop);
-    if (bvh_out) cudaFree(bvh_out);
-    if (hc) cudaFreeHost(hc);
+    pool_free(tris, tris_bytes, device);
+    pool_free(mat, mat_bytes, device);
+    pool_free(mat_prop, mat_prop_bytes, device);
+    pool_free(bvh_out, bvh_bytes, device);
+    pool_free_pinned(hc);
   }
 };
 
@@ -143,16 +231,19 @@ ams_status ams_scene_create(const float *tris, int n_tri, const int *mat, const 
   auto fail = [&](ams_status code) { delete s; return code; };
   cudaError_t e;
   if ((e = cudaEventCreate(&s->k2[0])) != cudaSuccess || (e = cudaEventCreate(&s->k2[1])) != cudaSuccess ||
-      (e = cudaMallocHost(&s->hc, sizeof(HostCounters))) != cudaSuccess) {
+      (e = pool_malloc_pinned(&s->hc)) != cudaSuccess) {
     set_err(errbuf, errlen, "cudaMallocHost: %s", cudaGetErrorString(e));
     return fail(AMS_ERR_OOM);
   }
-  size_t tb = sizeof(float) * 9 * (size_t)std::max(n_tri, 1);
-  if ((e = cudaMalloc(&s->tris, tb)) != cudaSuccess ||
-      (e = cudaMalloc(&s->mat, sizeof(int) * (size_t)std::max(n_tri, 1))) != cudaSuccess ||
-      (e = cudaMalloc(&s->mat_prop, sizeof(float) * 19 * (size_t)std::max(n_mat, 1))) !=
+  s->tris_bytes = sizeof(float) * 9 * (size_t)std::max(n_tri, 1);
+  s->mat_bytes = sizeof(int) * (size_t)std::max(n_tri, 1);
+  s->mat_prop_bytes = sizeof(float) * 19 * (size_t)std::max(n_mat, 1);
+  s->bvh_bytes = lbvh_output_bytes(n_tri);
+  if ((e = pool_malloc(reinterpret_cast<void **>(&s->tris), s->tris_bytes)) != cudaSuccess ||
+      (e = pool_malloc(reinterpret_cast<void **>(&s->mat), s->mat_bytes)) != cudaSuccess ||
+      (e = pool_malloc(reinterpret_cast<void **>(&s->mat_prop), s->mat_prop_bytes)) !=
           cudaSuccess ||
-      (e = cudaMalloc(&s->bvh_out, lbvh_output_bytes(n_tri))) != cudaSuccess) {
+      (e = pool_malloc(reinterpret_cast<void **>(&s->bvh_out), s->bvh_bytes)) != cudaSuccess) {
     set_err(errbuf, errlen, "scene allocation: %s", cudaGetErrorString(e));
     return fail(AMS_ERR_OOM);
   }
