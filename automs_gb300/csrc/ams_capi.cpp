@@ -817,9 +817,14 @@ ams_status ams_coverage_db(const float *H, int S, int R, float threshold, float 
 }
 
 unsigned long long ams_scratch_bytes(void) {
-  std::lock_guard<std::mutex> lk(g_scratch_mu);
   unsigned long long t = 0;
-  for (auto &d : g_scratch) t += d.cap;
+  {
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    for (auto &d : g_scratch) t += d.cap;
+  }
+  BlockPool &bp = block_pool();
+  std::lock_guard<std::mutex> lk(bp.mu);
+  for (auto &kv : bp.free_blocks) t += kv.first.second;
   return t;
 }
 

@@ -266,8 +266,9 @@ ams_status ams_mlp_adam_state(ams_mlp *mlp, float *m1, float *m2,
                               long long *step, int direction, void *stream,
                               char *errbuf, size_t errlen);
 
-/* Device bytes held by the library's internal scratch (all objective calls
- * on this device) -- for leak checks. */
+/* Device bytes held by the library itself: the objective's internal scratch
+ * (all devices) and the blocks of destroyed scenes kept for reuse by the
+ * next scene -- for leak checks. */
 unsigned long long ams_scratch_bytes(void);
 
 #ifdef __cplusplus
