@@ -1035,28 +1035,11 @@ cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *U, float *Yp
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
-// try_wait with a suspend-time hint: the thread sleeps until the phase
-// completes or the hint runs out instead of spinning (spinning warps took
-// issue slots from the other CTA on the SM); the 2 s bound is checked after
-// each wake-up
-constexpr uint32_t kSuspendNs = 1000000u;
+// bounded mbarrier wait of the tcgen05 kernels (tc_ptx.cuh): try_wait with a
+// suspend-time hint, so waiting warps sleep instead of taking issue slots
+// from the other CTA on the SM; false after 2 s
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-  unsigned long long t0 = 0;
-  for (uint32_t it = 0;; it++) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity), "r"(kSuspendNs)
-        : "memory");
-    if (ok) return true;
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    if (it == 0) t0 = t;
-    else if (t - t0 > 2000000000ull) return false;  // 2 s
-  }
+  return tc::mbar_wait(bar, parity);
 }
 
 template <int CB, int TR, int KPT>

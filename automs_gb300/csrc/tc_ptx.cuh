@@ -42,12 +42,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// bounded wait; false when the phase has not completed after limit_ns
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          unsigned long long limit_ns = kWaitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = now_ns();
   while (!mbar_try_wait(bar, parity))
-    if (now_ns() - t0 > kWaitNs) return false;
+    if (now_ns() - t0 > limit_ns) return false;
   return true;
 }
 // 2-D tiled TMA load; x (the contiguous coordinate) must be a multiple of
