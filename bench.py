@@ -149,6 +149,19 @@ def cpu_tracer_sample(cfg, threads):
     return st["rx_paths"], dt
 
 
+def aggregate_over_ranks(torch, dist, device, elapsed, units):
+    """Whole-job figures of N independent replicas (one seeded scene per
+    rank, no collective on the data path): the slowest rank's elapsed time
+    and the units all ranks processed.  dist is None for one process."""
+    if dist is None:
+        return elapsed, units
+    t = torch.tensor([float(elapsed)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t), float(u)
+
+
 def run_reference(args, rank, world):
     """The reference path's CPU restatement (oracle port, all host threads)."""
     if rank != 0:
@@ -679,12 +692,8 @@ def main():
     total_ms = sum(ms)
     paths = sum(s["rx_paths"] for _, _, s in steps)
     st0 = steps[0][2]
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        p = torch.tensor([float(paths)], device="cuda")
-        dist.all_reduce(p, op=dist.ReduceOp.SUM)
-        total_ms, paths = float(t), float(p)
+    total_ms, paths = aggregate_over_ranks(torch, dist if world > 1 else None, "cuda",
+                                           total_ms, paths)
     value = paths / (total_ms * 1e-3)
     if args.only == "tracer":
         print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": total_ms / args.steps,
@@ -714,7 +723,9 @@ def main():
         if k >= args.warmup:
             e2e_paths += st["rx_paths"]
             e2e_t += dt
-    e2e = {"value": e2e_paths / e2e_t * world, "unit": UNIT, "h2d_bytes_per_step": h2d,
+    e2e_t, e2e_paths = aggregate_over_ranks(torch, dist if world > 1 else None, "cuda", e2e_t,
+                                            e2e_paths)
+    e2e = {"value": e2e_paths / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h,
            "note": "Scene creation (copies + triangle BVH) + trace + result download per step"}
 
