@@ -7,7 +7,8 @@
 //   2. 30-bit Morton codes of the centroids scaled to a cube, with the
 //      primitive index in the low word (bit 30 set for primitives larger
 //      than a quarter of the scene),
-//   3. a stable LSD radix sort (one 1024-thread CTA, 4-bit digits, warp
+//   3. a sort of the keys: bitonic in shared memory up to 16,384 keys, else
+//      a stable LSD radix sort (one 1024-thread CTA, 4-bit digits, warp
 //      ballots for the in-tile ranks),
 //   4. the Karras hierarchy, one thread per internal node,
 //   5. a bottom-up refit with per-node arrival counters.
@@ -145,6 +146,33 @@ __global__ void __launch_bounds__(1024) k_sort(uint64_t *a, uint64_t *b, int n) 
     uint64_t *t = in; in = out; out = t;
   }
   // 8 passes: the sorted data is back in `a`
+}
+
+// Up to kSmemSortMax keys: bitonic sort in shared memory, one CTA of 1024
+// threads (log2(n) (log2(n) + 1) / 2 compare-exchange steps).  The keys are
+// unique (primitive index in the low word), so the order equals the stable
+// radix sort's.  Padding slots hold ~0, which sorts last.
+constexpr int kSmemSortMax = 16384;
+__global__ void __launch_bounds__(1024) k_sort_smem(uint64_t *a, int n) {
+  extern __shared__ uint64_t sk[];
+  int np = 1;
+  while (np < n) np <<= 1;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) sk[i] = i < n ? a[i] : ~0ull;
+  __syncthreads();
+  for (int k = 2; k <= np; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        const int l = i ^ j;
+        if (l > i) {
+          const uint64_t x = sk[i], y = sk[l];
+          const bool up = (i & k) == 0;
+          if ((x > y) == up) { sk[i] = y; sk[l] = x; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) a[i] = sk[i];
 }
 
 __device__ __forceinline__ int delta(const uint64_t *k, int n, int i, int j) {
@@ -324,7 +352,24 @@ static cudaError_t build_common(Lbvh &out, int n, char *scratch, char *outbuf,
   if (n == 0) return cudaSuccess;
   k_bounds<<<1, 1024, 0, st>>>(boxes, n, b6);
   k_morton<<<nblk(n, 256), 256, 0, st>>>(boxes, n, b6, ka);
-  k_sort<<<1, 1024, 0, st>>>(ka, kb, n);
+  if (n <= kSmemSortMax) {
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!attr_set[dev]) {
+      e = cudaFuncSetAttribute(k_sort_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               kSmemSortMax * (int)sizeof(uint64_t));
+      if (e != cudaSuccess) return e;
+      attr_set[dev] = true;
+    }
+    int np = 1;
+    while (np < n) np <<= 1;
+    k_sort_smem<<<1, 1024, np * sizeof(uint64_t), st>>>(ka, n);
+  } else {
+    k_sort<<<1, 1024, 0, st>>>(ka, kb, n);
+  }
   if (n > 1) {
     k_karras<<<nblk(n - 1, 256), 256, 0, st>>>(ka, n, out.nodes, parent);
     cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)n, st);
