@@ -159,15 +159,15 @@ __global__ void __launch_bounds__(1024) k_sort_smem(uint64_t *a, int n) {
   while (np < n) np <<= 1;
   for (int i = threadIdx.x; i < np; i += blockDim.x) sk[i] = i < n ? a[i] : ~0ull;
   __syncthreads();
+  // each step visits its np / 2 compare-exchange pairs (i, i + j) directly
   for (int k = 2; k <= np; k <<= 1) {
     for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = threadIdx.x; i < np; i += blockDim.x) {
-        const int l = i ^ j;
-        if (l > i) {
-          const uint64_t x = sk[i], y = sk[l];
-          const bool up = (i & k) == 0;
-          if ((x > y) == up) { sk[i] = y; sk[l] = x; }
-        }
+      for (int q = threadIdx.x; q < (np >> 1); q += blockDim.x) {
+        const int i = ((q & ~(j - 1)) << 1) | (q & (j - 1));
+        const int l = i + j;
+        const uint64_t x = sk[i], y = sk[l];
+        const bool up = (i & k) == 0;
+        if ((x > y) == up) { sk[i] = y; sk[l] = x; }
       }
       __syncthreads();
     }
