@@ -39,7 +39,7 @@ void set_err(char *buf, size_t len, const char *fmt, ...) {
 // cudaFree synchronises the whole device and cudaMalloc costs tens of
 // microseconds; a caller that builds a scene per channel (as build_channel,
 // go.py:679-767, does) would pay both on every call.  Blocks are kept in
-// power-of-two size classes per device.  A scene hands its blocks back only
+// size classes per device.  A scene hands its blocks back only
 // when it is destroyed, after its last call returned (every scene call
 // synchronises its stream), so no GPU work still uses them.  On an
 // allocation failure the device's cached blocks are released and the
@@ -53,9 +53,16 @@ BlockPool &block_pool() {
   static BlockPool *p = new BlockPool();  // lives until the process exits
   return *p;
 }
+// power-of-two classes from 4 KB; from 1 MB on, sixteenths of the power of
+// two above the request (at most 12.5% over: a 4.3 GB accumulator takes
+// 4.8 GB, not 8 GB)
 size_t size_class(size_t bytes) {
   size_t c = 4096;
   while (c < bytes) c <<= 1;
+  if (c >= ((size_t)1 << 20)) {
+    const size_t step = c / 16;
+    c = (bytes + step - 1) / step * step;
+  }
   return c;
 }
 cudaError_t pool_malloc(void **out, size_t bytes) {
