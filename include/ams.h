@@ -77,11 +77,18 @@ typedef struct {
 
 /* Create a scene from device arrays: tris [n_tri*9] float (3 vertices per
  * triangle), mat [n_tri] int32 material ids, mat_prop [n_mat*19] float
- * (angle-bin coefficients, negative = penetrable).  The arrays are copied.
+ * (angle-bin coefficients, negative = penetrable).  The arrays are copied
+ * (after the work queued on `stream`); material ids outside [0, n_mat) and
+ * non-finite coordinates are rejected with AMS_ERR_ARG.  The triangle
+ * hierarchy is built once here: a GPU LBVH below 16,384 triangles, a
+ * binned-SAH tree built on host threads from there on.  Synchronous.
  * Replaces the scene part of optixPathTracer.cpp:382-546. */
 ams_status ams_scene_create(const float *tris, int n_tri, const int *mat,
                             const float *mat_prop, int n_mat, void *stream,
                             ams_scene **out, char *errbuf, size_t errlen);
+/* The scene's device memory goes back to a per-device pool that the next
+ * scene draws from (no cudaFree, so no device-wide synchronisation); call
+ * only after the scene's last call returned. */
 void ams_scene_destroy(ams_scene *scene);
 
 /* Build the channel from src [s0*s1*3] to dst [n0*n1*3] (device float) and
