@@ -455,6 +455,15 @@ struct Slot {
   int ttl;
 };
 
+// image matrix of a branch slot; slot 0 is the primary ray (identity)
+__device__ __forceinline__ Mat34 slot_matrix(const Slot *slots, int i) {
+  if (i != 0) return slots[i].M;
+  Mat34 I;
+#pragma unroll
+  for (int k = 0; k < 12; k++) I.m[k] = (k == 0 || k == 5 || k == 10) ? 1.0f : 0.0f;
+  return I;
+}
+
 
 
 // Stage 1 runs as a persistent loop per warp with dynamic fetching (after
@@ -547,7 +556,7 @@ __device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, 
     c.ttl = w.ttl;
     c.o = o;
     c.d = sub3(d, scl3(N, 2.0f * dot3(d, N)));
-    c.M = slots[w.cur].M;
+    c.M = slot_matrix(slots, w.cur);
     af3 V = sub3(v0, image_of(c.M, w.spos));
     af3 Nimg = faceforward3(N0, V, N0);
     image_update(c.M, Nimg, v0);
@@ -567,7 +576,7 @@ __device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, 
         if (w.key_cur != w.cur || w.key_ttl != w.ttl) {
           int32_t key[14];
 #pragma unroll
-          for (int k = 0; k < 12; k++) key[k] = fbits(slots[w.cur].M.m[k]);
+          for (int k = 0; k < 12; k++) key[k] = fbits(slot_matrix(slots, w.cur).m[k]);
           key[12] = hc;
           key[13] = w.cur;
           slot = path_insert(P, key);
@@ -618,13 +627,16 @@ __device__ __forceinline__ bool s1_next(const TraceDev &P, S1Query &q, S1Ray &w,
       uint32_t src = (uint32_t)rs;
       if (src >= (uint32_t)P.n_src) src = (uint32_t)P.n_src - 1u;
       w.spos = ld3(P.src + 3 * src);
-      slots[0].o = w.spos;
-      slots[0].d = rand_dir(w.seed, (uint32_t)w.ix, (uint32_t)w.iy, P.launch_x, P.launch_y);
-#pragma unroll
-      for (int k = 0; k < 12; k++) slots[0].M.m[k] = (k == 0 || k == 5 || k == 10) ? 1.0f : 0.0f;
-      slots[0].ttl = P.L + 1;
-      w.pending = 1u;
-      w.key_cur = -1;  // slot 0 holds a new ray: forget the last key
+      // slot 0 (the primary ray) starts at once: origin and direction go
+      // straight into the query, and its image matrix is the identity,
+      // which is never stored (slot_matrix)
+      q.r.o = w.spos;
+      q.r.d = rand_dir(w.seed, (uint32_t)w.ix, (uint32_t)w.iy, P.launch_x, P.launch_y);
+      w.cur = 0;
+      w.ttl = P.L + 1;
+      w.guard = 0;
+      w.pending = 0u;
+      w.key_cur = -1;  // a new ray: forget the last key
       continue;
     }
     if (w.li >= 0 && w.capped) my_capped++;
