@@ -5,13 +5,15 @@ Run in a container where the reference tree is mounted (default
 
     python tests/golden/make_golden.py
 
-Two sources:
+Three sources:
   * channel fixtures: the reference's own device programs
     (optixPathTracer.cu) compiled for the CPU by oracle/ref_harness and run
     on seeded synthetic scenes (cases in tests/golden/cases.py);
   * objective fixtures: the reference's own go.Model (go.py:27-245) imported
     with stub matplotlib / numpy-stl modules and run on the CPU, loss and
-    autograd gradients recorded.
+    autograd gradients recorded;
+  * geometry fixtures: the reference's geometry helpers (go.py:248-512,
+    1309-1338) on seeded inputs, imported the same way.
 Outputs are small .npz files; the inputs are regenerated from the case
 definitions, whose sha256 is stored alongside to catch generator drift.
 """
@@ -184,6 +186,75 @@ def make_objective_fixtures():
             print(name, "loss", loss.item(), "dropped rows", int(drop.sum()))
 
 
+# ------------------------------------------------------------- geometry
+def geometry_inputs():
+    """Seeded inputs of the geometry helpers (go.py:248-512, 1309-1338)."""
+    rng = np.random.Generator(np.random.PCG64(11))
+
+    def unit(v):
+        v = np.asarray(v, np.float64)
+        return (v / np.linalg.norm(v)).tolist()
+
+    def frame():
+        k = np.array(unit(rng.normal(size=3)))
+        i = rng.normal(size=3)
+        i = i - (i @ k) * k
+        return unit(k), unit(i)
+    dirs = []
+    for n in range(40):
+        up = unit(rng.normal(size=3))
+        pol = unit(rng.normal(size=3))
+        th, ph = float(rng.uniform(-90, 90)), float(rng.uniform(0, 360))
+        if n % 2:
+            dirs.append((th / 180 * np.pi, ph / 180 * np.pi, up, pol, "rad"))
+        else:
+            dirs.append((th, ph, up, pol, "deg"))
+    mats = []
+    for size, spacing in (((3, 5), 0.0025), ((4, 4), 0.1), ((1, 6), 0.05), ((7, 2), 0.3)):
+        k, i = frame()
+        mats.append((rng.uniform(-5, 5, 3).tolist(), k, i, size, spacing))
+    mss = []
+    for size, spacing, th in (((4, 6), 0.0025, 0.001), ((3, 3), 0.2, 0.01), ((8, 5), 0.01, 0.002)):
+        k, i = frame()
+        mss.append((rng.uniform(-5, 5, 3).tolist(), k, i, size, spacing, th))
+    walls = []
+    for _ in range(6):
+        ul = rng.uniform(-5, 5, 3)
+        dl = ul + rng.uniform(-3, 3, 3)
+        dr = dl + rng.uniform(-3, 3, 3)
+        walls.append(([ul.tolist(), dl.tolist(), dr.tolist()],
+                      (float(rng.uniform(0, 1)), float(rng.uniform(0, 1)))))
+    ends = [([0.0, 1.0, 5], [2.0, 3.0, 4], 1.5), (0.5, [-1.0, 1.0, 3], [0.0, 2.0, 6]),
+            ([1.0, 2.0, 3], 0.25, [3.0, 1.0, 4])]
+    boxes = [([1.0, 2.0, 0.5], 0.2, 0.2, 1.5), ([-3.0, 0.5, 1.0], 0.7, 1.3, 0.4),
+             ([0.0, 0.0, 0.0], 2.0, 1.0, 3.0)]
+    return dict(dirs=dirs, mats=mats, mss=mss, walls=walls, ends=ends, boxes=boxes)
+
+
+def make_geometry_fixtures():
+    g = geometry_inputs()
+    out = {}
+    with reference_go_on_cpu() as (go, _):
+        for n, (th, ph, up, pol, u) in enumerate(g["dirs"]):
+            out[f"dir{n}"] = go.gen_direction_from_angle(th, ph, up, pol, unit=u).numpy()
+        for n, (c, k, i, size, sp) in enumerate(g["mats"]):
+            out[f"mat{n}"] = go.gen_pos_matrix(c, k, i, size, sp).numpy()
+        for n, (c, k, i, size, sp, th) in enumerate(g["mss"]):
+            pos, bh, kd = go.gen_ms(c, k, i, size, sp, th)
+            out[f"ms{n}_pos"] = pos.numpy()
+            out[f"ms{n}_bh"] = np.asarray(bh, np.float32)
+            out[f"ms{n}_k"] = kd.numpy()
+        for n, (w, ij) in enumerate(g["walls"]):
+            v, kd, idir = go.gen_sth_from_wall(w, ij)
+            out[f"wall{n}"] = np.stack([v.numpy(), kd.numpy(), idir.numpy()])
+        for n, (x, y, z) in enumerate(g["ends"]):
+            out[f"end{n}"] = go.gen_pos_from_endpoint(x, y, z).numpy()
+        for n, (c, xl, yl, zl) in enumerate(g["boxes"]):
+            out[f"box{n}"] = np.asarray(go.create_vertex_buffer(c, xl, yl, zl), np.float32)
+    np.savez_compressed(os.path.join(HERE, "geometry_ref.npz"), **out)
+    print("geometry fixtures written:", len(out))
+
+
 if __name__ == "__main__":
     if not oracle.ref_available():
         raise SystemExit("reference tree not mounted; fixtures cannot be regenerated here")
@@ -193,3 +264,4 @@ if __name__ == "__main__":
     make_unit_fixtures()
     make_channel_fixtures()
     make_objective_fixtures()
+    make_geometry_fixtures()
