@@ -231,10 +231,42 @@ def geometry_inputs():
     return dict(dirs=dirs, mats=mats, mss=mss, walls=walls, ends=ends, boxes=boxes)
 
 
+def write_scene_text_files(folder):
+    """Seeded ap.txt, door.txt and wall.txt in the reference's formats
+    (go.py:533-620): ap = centre line + direction line; a door = 3 vertex
+    lines + a 0/1 swing line; a wall = a name line + 3 vertex lines."""
+    rng = np.random.Generator(np.random.PCG64(12))
+    fmt = lambda v: " ".join(f"{x:.6f}" for x in v)
+    with open(os.path.join(folder, "ap.txt"), "w") as f:
+        f.write(fmt(rng.uniform(0, 10, 3)) + "\n" + fmt(rng.normal(size=3)) + "\n")
+    with open(os.path.join(folder, "door.txt"), "w") as f:
+        for d in range(3):
+            base = rng.uniform(0, 10, 3)
+            base[2] = 0.0
+            f.write(fmt(base + [0, 0, 2.1]) + "\n" + fmt(base) + "\n")
+            f.write(fmt(base + np.append(rng.uniform(-1, 1, 2), 0.0)) + "\n" + f"{d % 2}\n")
+    with open(os.path.join(folder, "wall.txt"), "w") as f:
+        for w in range(4):
+            f.write(f"wall{w}\n")
+            for _ in range(3):
+                f.write(fmt(rng.uniform(-5, 5, 3)) + "\n")
+
+
+DOOR_ANGLES = (0.0, 0.3, -1.2)
+
+
 def make_geometry_fixtures():
+    import tempfile
     g = geometry_inputs()
     out = {}
     with reference_go_on_cpu() as (go, _):
+        with tempfile.TemporaryDirectory() as d:
+            write_scene_text_files(d)
+            c, k = go.get_ap(d)
+            out["ap"] = np.asarray([c, k], np.float64)
+            for n, ang in enumerate(DOOR_ANGLES):
+                out[f"doors{n}"] = np.asarray(go.get_doors(d, ang), np.float64)
+            out["walls"] = np.asarray(go.get_walls(d), np.float64)
         for n, (th, ph, up, pol, u) in enumerate(g["dirs"]):
             out[f"dir{n}"] = go.gen_direction_from_angle(th, ph, up, pol, unit=u).numpy()
         for n, (c, k, i, size, sp) in enumerate(g["mats"]):

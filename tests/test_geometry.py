@@ -6,7 +6,7 @@ import os
 import numpy as np
 
 from automs_gb300 import geometry as G
-from make_golden import geometry_inputs
+from make_golden import DOOR_ANGLES, geometry_inputs, write_scene_text_files
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "geometry_ref.npz")
 
@@ -38,3 +38,13 @@ def test_geometry_helpers_match_reference():
         close(G.gen_pos_from_endpoint(x, y, z, **cpu), g[f"end{n}"])
     for n, (c, xl, yl, zl) in enumerate(inp["boxes"]):
         close(np.asarray(G.create_vertex_buffer(c, xl, yl, zl), np.float32), g[f"box{n}"])
+
+
+def test_scene_text_files_match_reference(tmp_path):
+    g = np.load(GOLD)
+    write_scene_text_files(str(tmp_path))
+    c, k = G.get_ap(str(tmp_path))
+    assert np.array_equal(np.asarray([c, k], np.float64), g["ap"])
+    for n, ang in enumerate(DOOR_ANGLES):
+        assert np.array_equal(np.asarray(G.get_doors(str(tmp_path), ang), np.float64), g[f"doors{n}"])
+    assert np.array_equal(np.asarray(G.get_walls(str(tmp_path)), np.float64), g["walls"])
