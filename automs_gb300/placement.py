@@ -173,9 +173,14 @@ def score(gain):
     return gain.mean(-1)
 
 
-def anneal_candidates(study, n, rng, surrogate=None, t0=1.0, t1=0.02):
-    """Simulated-annealing chain over placements.  With a surrogate, moves are
-    accepted on its predicted score; every visited placement is returned."""
+def anneal_candidates(study, n, rng, surrogate=None, t0=1.0, t1=0.02, device="cuda"):
+    """Simulated-annealing chain over placements (the NNI Anneal tuner's role,
+    physical_exp_nni_main.py:11-29).  Moves: another wall with probability
+    0.1, the position (u, v) by N(0, 0.08) clipped to [0.1, 0.9], the size by
+    +-8 with probability 0.2 within study.sizes.  With a surrogate (a callable
+    on descriptors placed on `device`), moves are accepted on its predicted
+    score by the Metropolis rule at a temperature falling geometrically from
+    t0 to t1; every visited placement is returned."""
     cur = study.random_params(rng)
     visited = [cur]
     cur_s = None
@@ -195,7 +200,7 @@ def anneal_candidates(study, n, rng, surrogate=None, t0=1.0, t1=0.02):
                 s = int(np.clip(s + 8 * rng.choice([-1, 1]), lo, hi))
             props.append((w, u, v, s))
         if surrogate is not None:
-            X = torch.as_tensor(np.stack([study.descriptor(q) for q in props]), device="cuda")
+            X = torch.as_tensor(np.stack([study.descriptor(q) for q in props]), device=device)
             sc = score(surrogate(X)).cpu().numpy()
         else:
             sc = rng.normal(size=len(props))
