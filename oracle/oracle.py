@@ -115,9 +115,11 @@ def aabbs(pos, r):
     return np.concatenate([pos - r32, pos + r32], axis=-1).astype(np.float32)
 
 
-def trace_channel(tris, mat, mat_prop, src, dst, params, nthreads=0, max_paths=1 << 20):
-    """Oracle build_channel.  src [s0,s1,3], dst [n0,n1,3].  Returns
-    (H complex64 [S,R], stats dict, paths int32 [P,14])."""
+def trace_channel(tris, mat, mat_prop, src, dst, params, nthreads=0, max_paths=1 << 20,
+                  src_box=None, dst_box=None):
+    """Oracle build_channel.  src [s0,s1,3], dst [n0,n1,3]; src_box / dst_box
+    (float32 [n, 6]) default to pos -/+ r.  Returns (H complex64 [S,R],
+    stats dict, paths int32 [P,14])."""
     L = lib()
     tris = _c(tris, np.float32).reshape(-1, 9)
     mat = _c(mat, np.int32).reshape(-1)
@@ -127,8 +129,10 @@ def trace_channel(tris, mat, mat_prop, src, dst, params, nthreads=0, max_paths=1
     n_src = src.size // 3
     n0, n1 = dst.shape[0], dst.shape[1]
     n_dst = n0 * n1
-    src_box = aabbs(src, params.get("src_r", 0.5e-5))
-    dst_box = aabbs(dst, params.get("dst_r", 0.06))
+    src_box = (aabbs(src, params.get("src_r", 0.5e-5)) if src_box is None
+               else _c(src_box, np.float32).reshape(-1, 6))
+    dst_box = (aabbs(dst, params.get("dst_r", 0.06)) if dst_box is None
+               else _c(dst_box, np.float32).reshape(-1, 6))
     res = np.zeros((n_src, n_dst, 2), np.float32)
     st = OrcStats()
     paths = np.zeros((max_paths, 14), np.int32)
@@ -148,10 +152,12 @@ def trace_channel(tris, mat, mat_prop, src, dst, params, nthreads=0, max_paths=1
     return (res[..., 0] + 1j * res[..., 1]).astype(np.complex64), stats, paths[:npaths].copy()
 
 
-def ref_trace_channel(tris, mat, mat_prop, src, dst, params, max_paths=1 << 20):
+def ref_trace_channel(tris, mat, mat_prop, src, dst, params, max_paths=1 << 20, src_box=None,
+                      dst_box=None):
     """The reference device programs run on the CPU (oracle/_ref).  Same
     return convention as trace_channel; stats has rx_paths, rx_fail,
-    fwd_records, unique_records, unique_paths, rounds."""
+    fwd_records, unique_records, unique_paths, rounds.  src_box / dst_box
+    (float32 [n, 6]) default to pos -/+ r."""
     R = ref_lib()
     tris = _c(tris, np.float32).reshape(-1, 9)
     mat = _c(mat, np.int32).reshape(-1)
@@ -160,8 +166,10 @@ def ref_trace_channel(tris, mat, mat_prop, src, dst, params, max_paths=1 << 20):
     dst = _c(dst, np.float32)
     s0, s1 = src.shape[0], src.shape[1]
     n0, n1 = dst.shape[0], dst.shape[1]
-    src_box = aabbs(src, params.get("src_r", 0.5e-5))
-    dst_box = aabbs(dst, params.get("dst_r", 0.06))
+    src_box = (aabbs(src, params.get("src_r", 0.5e-5)) if src_box is None
+               else _c(src_box, np.float32).reshape(-1, 6))
+    dst_box = (aabbs(dst, params.get("dst_r", 0.06)) if dst_box is None
+               else _c(dst_box, np.float32).reshape(-1, 6))
     res = np.zeros((s0 * s1, n0 * n1, 2), np.float32)
     stats = np.zeros(2, np.uint64)
     counts = np.zeros(4, np.int64)

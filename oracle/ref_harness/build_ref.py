@@ -4,8 +4,9 @@ Recipe: g++ on optixPathTracer.cu where it lies in the reference tree, with
 the OptiX shim of oracle/ref_harness/shim first on the include path and the
 reference's vendored sutil / random.h headers after it.  Output goes to
 oracle/_ref/libams_ref.so (git-ignored).  Nothing is copied out of the
-reference tree.  This only runs where the reference tree is mounted; the
-fixtures it produces are committed under tests/golden/.
+reference tree.  The reference tree is named by the environment variable
+AMS_REFERENCE_ROOT; without it the harness is not built (available() is
+False).  The fixtures it produces are committed under tests/golden/.
 """
 import os
 import subprocess
@@ -14,16 +15,22 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 OUT = os.path.join(ORACLE, "_ref")
 LIB = os.path.join(OUT, "libams_ref.so")
-REF = os.environ.get("AMS_REFERENCE_ROOT", "/root/reference")
-CUDA_INC = "/usr/local/cuda/include"
+CUDA_INC = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+
+
+def ref_root():
+    """The reference tree named by AMS_REFERENCE_ROOT, or None."""
+    r = os.environ.get("AMS_REFERENCE_ROOT")
+    return r if r and os.path.exists(os.path.join(r, "optixPathTracer.cu")) else None
 
 
 def available():
-    return os.path.exists(os.path.join(REF, "optixPathTracer.cu"))
+    return ref_root() is not None
 
 
 def build_ref(force=False):
-    if not available():
+    REF = ref_root()
+    if REF is None:
         return None
     os.makedirs(OUT, exist_ok=True)
     srcs = [os.path.join(HERE, "ref_harness.cpp"), os.path.join(ORACLE, "ams_oracle.c")]

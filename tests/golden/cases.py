@@ -127,3 +127,41 @@ def objective_case(name):
     return dict(channels=ch, theta=theta, phi=phi, n_ms=len(Ms), max_ms_reflex=spec["reflex"],
                 code_num=spec["C"], w=spec["w"], max_phase_deg=spec["max_phase"],
                 seed=spec["seed"])
+
+
+# ------------------------------------------------- the reference's scene
+# A reduced channel set on the reference's own scene folder (stl/4321 of the
+# reference tree), placed as its single trial places AP, Rx and metasurface
+# (physical_exp_nni_model.py:26-87) but smaller: 2x2 AP, 20x18 Rx at one
+# height, two metasurfaces (6x8 on wall 1 at the trial's ms_j, and a 4x6
+# relay 1 m in front of it facing it, so that the ms0 -> ms1 trace finds
+# paths with the reference's 100 x 100 launch), a door and a reflector
+# quad, 3 reflections.
+REF_SCENE = "stl/4321"
+REF_SCENE_L = 3
+REF_SCENE_FLOOR = -1.4161
+
+
+def reference_scene_setup(go, folder, lam):
+    """Inputs of the reduced reference-scene channel set, made with the
+    reference's geometry helpers (module `go`)."""
+    walls = go.get_walls(folder)
+    center_a, k_a, _ = go.gen_sth_from_wall(walls[0], (0.5, 0.5))
+    center_a[2] = REF_SCENE_FLOOR + 2.5
+    ap_dir = go.gen_direction_from_angle(0, 23.4352 - 90, [0, 0, 1], [0, 1, 0])
+    src = go.gen_pos_matrix(center_a + k_a * 0.3, ap_dir, [0, 0, -1], (2, 2), lam * 0.58)
+    dst = go.gen_pos_from_endpoint([-6, 2.4, 20], [-1, 6.5, 18], REF_SCENE_FLOOR + 0.9)
+    c, k, i = go.gen_sth_from_wall(walls[1], (0.5, 0.11939808933765397))
+    c[2] = REF_SCENE_FLOOR + 2.0
+    pos, bh, n = go.gen_ms(c.clone(), k, i, (6, 8), lam / 2)
+    ms_list = [go.Metasurface(pos, (6, 8), n, n, bh, 300)]
+    pos, bh, n = go.gen_ms(c + k * 1.0, -k, i, (4, 6), lam / 2)
+    ms_list.append(go.Metasurface(pos, (4, 6), n, n, bh, 300))
+    z0, z1 = REF_SCENE_FLOOR, REF_SCENE_FLOOR + 2.1
+    door = [[[-3.0, 0.5, z1], [-3.0, 1.5, z1], [-3.0, 0.5, z0]],
+            [[-3.0, 0.5, z0], [-3.0, 1.5, z0], [-3.0, 1.5, z1]]]
+    r0, r1 = REF_SCENE_FLOOR + 0.9, REF_SCENE_FLOOR + 1.9
+    reflector = [[[-0.5, 1.0, r1], [-0.5, 2.0, r1], [-0.5, 1.0, r0]],
+                 [[-0.5, 1.0, r0], [-0.5, 2.0, r0], [-0.5, 2.0, r1]]]
+    return dict(src=src, dst=dst, ap_dir=ap_dir, ms_list=ms_list, door=[door],
+                reflector=[reflector])

@@ -1,9 +1,8 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Run in a container where the reference tree is mounted (default
-/root/reference, override with AMS_REFERENCE_ROOT):
+Run where the reference tree is mounted, naming it in AMS_REFERENCE_ROOT:
 
-    python tests/golden/make_golden.py
+    AMS_REFERENCE_ROOT=<reference tree> python tests/golden/make_golden.py
 
 Three sources:
   * channel fixtures: the reference's own device programs
@@ -20,6 +19,7 @@ definitions, whose sha256 is stored alongside to catch generator drift.
 import contextlib
 import ctypes as C
 import hashlib
+import json
 import os
 import sys
 import types
@@ -31,7 +31,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 sys.path.insert(0, HERE)
-REF = os.environ.get("AMS_REFERENCE_ROOT", "/root/reference")
+REF = os.environ.get("AMS_REFERENCE_ROOT")
 
 import cases  # noqa: E402
 import oracle  # noqa: E402
@@ -103,6 +103,27 @@ def make_unit_fixtures():
     print("unit fixtures written")
 
 
+class StubMesh:
+    """Stand-in for numpy-stl's mesh.Mesh (go.py:9, 700): from_file reads a
+    binary STL record by record with struct (independent of the package's
+    numpy reader, scenes.read_stl) and exposes .vectors [n, 3, 3] float32."""
+
+    def __init__(self, vectors):
+        self.vectors = vectors
+
+    @classmethod
+    def from_file(cls, path):
+        import struct
+        with open(path, "rb") as f:
+            data = f.read()
+        (n,) = struct.unpack_from("<I", data, 80)
+        out = np.zeros((n, 3, 3), np.float32)
+        for i in range(n):
+            rec = struct.unpack_from("<12fH", data, 84 + 50 * i)
+            out[i] = np.asarray(rec[3:12], np.float32).reshape(3, 3)
+        return cls(out)
+
+
 # ------------------------------------------------------------ objective
 @contextlib.contextmanager
 def reference_go_on_cpu():
@@ -113,6 +134,7 @@ def reference_go_on_cpu():
     for name in ("matplotlib", "matplotlib.pyplot", "stl", "stl.mesh"):
         stubs[name] = types.ModuleType(name)
     stubs["stl"].mesh = stubs["stl.mesh"]
+    stubs["stl.mesh"].Mesh = StubMesh
     stubs["matplotlib"].pyplot = stubs["matplotlib.pyplot"]
     saved_mods = {k: sys.modules.get(k) for k in stubs}
     sys.modules.update(stubs)
@@ -287,9 +309,100 @@ def make_geometry_fixtures():
     print("geometry fixtures written:", len(out))
 
 
+# ------------------------------------------------- the reference's scene
+def make_reference_scene_fixtures():
+    """go.py's own build_channels on the reference scene stl/4321, reduced
+    (cases.reference_scene_setup: 2x2 AP, 20x18 Rx, two metasurfaces, a
+    door and a reflector quad, 3 reflections, go.py's 100 x 100 launch): the
+    reference's ingest (go.py:679-737) and channel-set logic
+    (go.py:1135-1247) run as written, its OptiX op replaced by the
+    reference's device programs on the CPU (oracle/ref_harness).  Saved: the
+    scene folder's files in this folder's listdir order, the inputs, the
+    ingest of every trace (full arrays for the first, sha256 for all) and per
+    trace H, counters and the ordered path list."""
+    import torch
+    folder = os.path.join(REF, *cases.REF_SCENE.split("/"))
+    lam = 3e8 / 60e9
+    traces = []
+
+    def op(result, src, dst, src_buffer, dst_buffer, scene_buffer, mat, spl, lx, ly, wave_len,
+           L, reserve, mat_prop, src_dir, dst_dir, log_level, sbp, dbp, gs, src_r, dst_r):
+        params = dict(samples_per_launch=int(spl), launch_x=int(lx), launch_y=int(ly),
+                      wave_len=float(wave_len), max_reflection=int(L), reserve_size=int(reserve),
+                      src_bptype=int(sbp), dst_bptype=int(dbp), dst_gridsize=int(gs),
+                      src_r=float(src_r), dst_r=float(dst_r),
+                      src_dir=[float(x) for x in src_dir], dst_dir=[float(x) for x in dst_dir])
+        sb = scene_buffer.numpy().astype(np.float32)
+        H, st, paths = oracle.ref_trace_channel(sb.reshape(-1, 9), mat.numpy(), mat_prop.numpy(),
+                                                src.numpy(), dst.numpy(), params,
+                                                src_box=src_buffer.numpy(),
+                                                dst_box=dst_buffer.numpy())
+        result[..., 0] += torch.from_numpy(np.ascontiguousarray(H.real))
+        result[..., 1] += torch.from_numpy(np.ascontiguousarray(H.imag))
+        traces.append(dict(params=params, H=H, paths=paths,
+                           stats=np.array([st[k] for k in cases.STAT_KEYS], np.int64),
+                           ingest_sha=digest(sb, mat.numpy().astype(np.int32),
+                                             mat_prop.numpy().astype(np.float32)),
+                           n_tri=sb.shape[0] // 3,
+                           scene=(sb, mat.numpy().astype(np.int32),
+                                  mat_prop.numpy().astype(np.float32))))
+        print("  trace", len(traces), st, flush=True)
+
+    with reference_go_on_cpu() as (go, _):
+        setup = cases.reference_scene_setup(go, folder, lam)
+        saved_ops = torch.ops
+        torch.ops = types.SimpleNamespace(
+            pathtrace=types.SimpleNamespace(torch_launch_pathtrace=op))
+        try:
+            ch = go.build_channels(setup["src"], setup["dst"], setup["ms_list"], setup["ap_dir"],
+                                   folder, lam, cases.REF_SCENE_L,
+                                   reflector_buffer=setup["reflector"],
+                                   door_buffer=setup["door"])
+        finally:
+            torch.ops = saved_ops
+    keys = list(ch.keys())
+    assert len(keys) == len(traces)
+    names = [f for f in os.listdir(folder) if f.endswith(".stl")]
+    blocks = [StubMesh.from_file(os.path.join(folder, f)).vectors for f in names]
+    with open(os.path.join(folder, "mat.txt")) as f:
+        mat_txt = f.read()
+    with open(os.path.join(folder, "wall.txt")) as f:
+        wall_txt = f.read()
+    out = dict(stl_names=np.array(names), stl_counts=np.array([len(b) for b in blocks]),
+               stl_tris=np.concatenate(blocks, 0), mat_txt=np.array(mat_txt),
+               wall_txt=np.array(wall_txt), keys=np.array(keys),
+               src=setup["src"].numpy(), dst=setup["dst"].numpy(),
+               ap_dir=setup["ap_dir"].numpy(),
+               door=np.asarray(setup["door"], np.float32),
+               reflector=np.asarray(setup["reflector"], np.float32))
+    for i, m in enumerate(setup["ms_list"]):
+        out[f"ms{i}_pos"] = m.pos.numpy()
+        out[f"ms{i}_send"] = m.send_dir.numpy()
+        out[f"ms{i}_recv"] = m.recv_dir.numpy()
+        out[f"ms{i}_blackhole"] = np.asarray(m.blackhole, np.float32)
+        out[f"ms{i}_size"] = np.asarray(m.size)
+    sb, mt, mp = traces[0]["scene"]
+    out["scene0_buffer"], out["scene0_mat"], out["scene0_mat_prop"] = sb, mt, mp
+    for k, t in zip(keys, traces):
+        tag = k.replace("{", "").replace("}", "")
+        out[f"{tag}_H"] = t["H"]
+        out[f"{tag}_paths"] = t["paths"]
+        out[f"{tag}_stats"] = t["stats"]
+        out[f"{tag}_ingest_sha"] = np.array(t["ingest_sha"])
+        out[f"{tag}_n_tri"] = np.array(t["n_tri"])
+        out[f"{tag}_params"] = np.array(json.dumps(t["params"]))
+        assert np.array_equal(ch[k].numpy(), t["H"])
+    np.savez_compressed(os.path.join(HERE, "ref_scene_4321.npz"), **out)
+    print("reference-scene fixtures written:", keys)
+
+
 if __name__ == "__main__":
-    if not oracle.ref_available():
-        raise SystemExit("reference tree not mounted; fixtures cannot be regenerated here")
+    if not REF or not oracle.ref_available():
+        raise SystemExit("AMS_REFERENCE_ROOT does not name the reference tree; "
+                         "fixtures cannot be regenerated")
+    if sys.argv[1:] == ["ref_scene"]:
+        make_reference_scene_fixtures()
+        raise SystemExit(0)
     if len(sys.argv) > 1:  # regenerate the named channel fixtures only
         make_channel_fixtures(sys.argv[1:])
         raise SystemExit(0)
@@ -297,3 +410,4 @@ if __name__ == "__main__":
     make_channel_fixtures()
     make_objective_fixtures()
     make_geometry_fixtures()
+    make_reference_scene_fixtures()
