@@ -823,6 +823,43 @@ ams_status ams_coverage_db(const float *H, int S, int R, float threshold, float 
   return AMS_OK;
 }
 
+ams_status ams_objective_status(const ams_objective_plan *plan, void *stream, char *errbuf,
+                                size_t errlen) {
+  clear_stale_error();
+  CK(cudaStreamSynchronize((cudaStream_t)stream));
+  std::vector<const unsigned *> words;
+  if (plan) {
+    if (!plan->p) { set_err(errbuf, errlen, "plan is NULL"); return AMS_ERR_ARG; }
+    words.push_back(obj_tc_plan_status_word(plan->p));
+  } else {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    {
+      std::lock_guard<std::mutex> lk(g_scratch_mu);
+      if ((int)g_scratch.size() > dev && g_scratch[dev].ptr)
+        words.push_back(reinterpret_cast<const unsigned *>(g_scratch[dev].ptr + 48));
+    }
+    char *na = nullptr;
+    CK(obj_noalloc_scratch(&na));
+    words.push_back(reinterpret_cast<const unsigned *>(na + 48));
+  }
+  unsigned flags = 0;
+  for (const unsigned *w : words) {
+    unsigned v = 0;
+    CK(cudaMemcpy(&v, w, 4, cudaMemcpyDeviceToHost));
+    flags |= v;
+  }
+  if (flags) {
+    set_err(errbuf, errlen,
+            "a bounded wait of the last objective call ran out (flags 0x%x): its outputs are NaN",
+            flags);
+    return AMS_ERR_INTERNAL;
+  }
+  return AMS_OK;
+}
+
+void ams_debug_inject_wait_timeout(int calls) { obj_inject_timeouts(calls); }
+
 unsigned long long ams_scratch_bytes(void) {
   unsigned long long t = 0;
   {
@@ -952,7 +989,7 @@ ams_status ams_mlp_create(const int *dims, int n_dims, int max_batch, unsigned l
   for (int l = 0; l < d.L; l++) off_H[l] = add(2 * (size_t)d.max_bp * d.dp[l]);
   size_t off_tA = add(2 * (size_t)d.max_bp * maxw), off_tB = add(2 * (size_t)d.max_bp * maxw);
   size_t off_Y = add(4 * (size_t)d.max_bp * d.dp[d.L]);
-  size_t off_part = add(8 * 152 * 4), off_err = add(4);
+  size_t off_part = add(8 * (size_t)kMlpLossParts), off_err = add(4);
   cudaError_t e = cudaMalloc(&m->arena, total);
   if (e != cudaSuccess) {
     set_err(errbuf, errlen, "MLP arena (%zu bytes): %s", total, cudaGetErrorString(e));

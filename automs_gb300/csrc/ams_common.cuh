@@ -16,6 +16,40 @@
 #define AMS_MAX_L 5      // 32 branch slots (optixPathTracer.h:5)
 #define AMS_MAX_RESERVE 256
 
+// Facts of the current device, looked up once per device (up to 64 devices
+// per process).
+#define AMS_MAX_DEVICES 64
+inline int ams_current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= AMS_MAX_DEVICES) return -1;
+  return dev;
+}
+// multiprocessors of the current device (1 if the query fails)
+inline int ams_device_sms() {
+  static int sms[AMS_MAX_DEVICES] = {0};
+  const int dev = ams_current_device();
+  if (dev < 0) return 1;
+  if (sms[dev] == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 1;
+    sms[dev] = n;
+  }
+  return sms[dev];
+}
+// Raise a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes`; `cur` is the caller's per-kernel record of the limit set.
+template <class F>
+inline cudaError_t ams_set_smem_atleast(size_t (&cur)[AMS_MAX_DEVICES], F *kernel, size_t bytes) {
+  const int dev = ams_current_device();
+  if (dev < 0) return cudaErrorInvalidDevice;
+  if (cur[dev] >= bytes) return cudaSuccess;
+  cudaError_t e =
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur[dev] = bytes;
+  return e;
+}
+
 
 struct af3 { float x, y, z; };
 

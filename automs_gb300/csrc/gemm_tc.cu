@@ -167,13 +167,9 @@ cudaError_t launch(const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N,
   CUtensorMap ta, tb;
   if (!make_map_bf16(&ta, A, M, K, BM) || !make_map_bf16(&tb, B, N, K, BN)) return cudaErrorInvalidValue;
   const size_t smem = STAGES * (BM * BK * 2 + BN * BK * 2) + 1024;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
+  static size_t attr_set[AMS_MAX_DEVICES] = {0};
+  cudaError_t e = ams_set_smem_atleast(attr_set, k_gemm_tc<BN>, smem);
+  if (e != cudaSuccess) return e;
   dim3 grid(N / BN, M / BM);
   k_gemm_tc<BN><<<grid, 128, smem, st>>>(ta, tb, ep, K, err);
   return cudaGetLastError();

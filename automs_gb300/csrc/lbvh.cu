@@ -353,17 +353,9 @@ static cudaError_t build_common(Lbvh &out, int n, char *scratch, char *outbuf,
   k_bounds<<<1, 1024, 0, st>>>(boxes, n, b6);
   k_morton<<<nblk(n, 256), 256, 0, st>>>(boxes, n, b6, ka);
   if (n <= kSmemSortMax) {
-    static bool attr_set[64] = {false};
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    static size_t attr_set[AMS_MAX_DEVICES] = {0};
+    cudaError_t e = ams_set_smem_atleast(attr_set, k_sort_smem, kSmemSortMax * sizeof(uint64_t));
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    if (!attr_set[dev]) {
-      e = cudaFuncSetAttribute(k_sort_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               kSmemSortMax * (int)sizeof(uint64_t));
-      if (e != cudaSuccess) return e;
-      attr_set[dev] = true;
-    }
     int np = 1;
     while (np < n) np <<= 1;
     k_sort_smem<<<1, 1024, np * sizeof(uint64_t), st>>>(ka, n);

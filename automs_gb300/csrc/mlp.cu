@@ -201,7 +201,7 @@ cudaError_t mlp_backward(MlpDev &m, const float *T, int B, float *loss, cudaStre
   const int L = m.L;
   const int dl = m.d[L];
   // targets arrive as [B, d_L]; the output buffer has the same width
-  const int nblk = 152 * 4;
+  const int nblk = kMlpLossParts;
   k_loss<<<nblk, 256, 0, st>>>(m.Y, T, B, Bp, dl, 1.0f / ((float)B * dl), m.dZ[L], m.part);
   if (loss) k_loss_final<<<1, 32, 0, st>>>(m.part, nblk, 1.0f / ((double)B * dl), loss);
   cudaError_t e = cudaGetLastError();

@@ -6,6 +6,9 @@
 #include <cstdint>
 
 constexpr int kMlpMaxLayers = 8;
+// CTAs of the loss kernel, each writing one FP64 partial sum (a fixed work
+// split, so the loss is summed in the same order on every device)
+constexpr int kMlpLossParts = 608;
 
 struct MlpDev {
   int L = 0;                       // weight layers

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <mutex>
@@ -37,6 +38,12 @@ namespace {
 constexpr float kN0 = 1e-9f;                 // 10^(-90/10) mW, go.py:183-184
 constexpr float kEps = 1.1920928955078125e-07f;  // float32 eps, go.py:181
 constexpr float kInvLn2 = 1.4426950408889634f;
+// the value of every output of a call whose bounded wait ran out
+__device__ __forceinline__ float obj_nan() { return __int_as_float(0x7fc00000); }
+// a bounded wait of this call ran out (err may be NULL: a path without waits)
+__device__ __forceinline__ bool obj_failed(const unsigned *err) {
+  return err != nullptr && __ldcg(err) != 0u;
+}
 
 struct c2 { float x, y; };
 __device__ __forceinline__ c2 ld2(const float *p, size_t i) {
@@ -237,7 +244,8 @@ __device__ __forceinline__ void block_sum_pairs(const double *partials, int nb, 
 template <int CB>
 __global__ void __launch_bounds__(256) k_epilogue(ObjArgs a, int kspl, const float *Ypart,
                                                   float *G1, float *G2, double *partials,
-                                                  unsigned *counter, float *scal) {
+                                                  unsigned *counter, float *scal,
+                                                  const unsigned *err) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   float sum_max = 0.f, sum_sq = 0.f;  // FP32 within a warp, FP64 across warps
   if (r < a.R) {
@@ -312,7 +320,7 @@ __global__ void __launch_bounds__(256) k_epilogue(ObjArgs a, int kspl, const flo
     block_sum_pairs(partials, (int)gridDim.x, x, z);
     if (threadIdx.x == 0) {
       const double nrm = sqrt(z);
-      if (a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
+      if (a.loss) *a.loss = obj_failed(err) ? obj_nan() : (float)(-(double)a.w * x + nrm);
       scal[0] = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
       *counter = 0u;  // ready for the next call
     }
@@ -461,7 +469,8 @@ __device__ __forceinline__ void epi_cap(const ObjArgs &a, int c, c2 y, float &am
 template <int CB>
 __global__ void __launch_bounds__(256) k_tc_epi_a(ObjArgs a, int kspl, const float *Ypart,
                                                   float *maxr, int *argr, double *partials,
-                                                  unsigned *counter, float *scal) {
+                                                  unsigned *counter, float *scal,
+                                                  const unsigned *err) {
   constexpr int CPT = CB / 8;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int r = blockIdx.x * 32 + lane;
@@ -526,7 +535,7 @@ __global__ void __launch_bounds__(256) k_tc_epi_a(ObjArgs a, int kspl, const flo
     block_sum_pairs(partials, (int)gridDim.x, x, z);
     if (threadIdx.x == 0) {
       const double nrm = sqrt(z);
-      if (a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
+      if (a.loss) *a.loss = obj_failed(err) ? obj_nan() : (float)(-(double)a.w * x + nrm);
       scal[0] = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
       *counter = 0u;  // ready for the next call
     }
@@ -728,7 +737,7 @@ __global__ void __launch_bounds__(256) k_final(ObjArgs a, int M, int K, int rspl
 // dphi[m] = -sum_c Im(conj(G_U[c, m]) U[c, m]); a CTA takes 32 elements
 // (lanes) and its 8 warps split the codes
 __global__ void __launch_bounds__(256) k_tc_dphi(const float *GU, const float *U, int C, int M,
-                                                 int K, float *dphi) {
+                                                 int K, float *dphi, const unsigned *err) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int m = blockIdx.x * 32 + lane;
   float acc = 0.f;
@@ -745,7 +754,7 @@ __global__ void __launch_bounds__(256) k_tc_dphi(const float *GU, const float *U
     float t = 0.f;
 #pragma unroll
     for (int w2 = 0; w2 < 8; w2++) t += red[w2][lane];
-    dphi[m] = -t;
+    dphi[m] = obj_failed(err) ? obj_nan() : -t;
   }
 }
 
@@ -798,7 +807,7 @@ __global__ void __launch_bounds__(128) k_tc_dw_part(const float *GU, const float
 }
 
 __global__ void k_tc_dw_sum(const float *GU, const float *dwp, int C, int S, int M, int K,
-                            float *grad_W) {
+                            float *grad_W, const unsigned *err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= C * S) return;
   const int c = i / S, s2 = i % S;
@@ -808,6 +817,7 @@ __global__ void k_tc_dw_sum(const float *GU, const float *dwp, int C, int S, int
     t.x += v.x;
     t.y += v.y;
   }
+  if (obj_failed(err)) t = make_float2(obj_nan(), obj_nan());
   reinterpret_cast<float2 *>(grad_W)[i] = t;
 }
 
@@ -825,8 +835,11 @@ template <int CB>
 __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int nparts,
                                                       const float *Ppart, const double *lpart,
                                                       const float *U, float *GU, float *dwp,
-                                                      unsigned *counter) {
+                                                      unsigned *counter, const unsigned *err) {
   constexpr int NW = 32;
+  // a bounded wait of the streaming kernel ran out: its partials are
+  // incomplete, so every output of the call is NaN
+  const bool bad = obj_failed(err);
   const int K = M + a.S;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + lane;
@@ -843,7 +856,7 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
     if (lane == 0) {
       const double nrm = sqrt(z);
       inv_s = nrm > 0 ? (float)(1.0 / nrm) : 0.f;
-      if (blockIdx.x == 0 && a.loss) *a.loss = (float)(-(double)a.w * x + nrm);
+      if (blockIdx.x == 0 && a.loss) *a.loss = bad ? obj_nan() : (float)(-(double)a.w * x + nrm);
     }
   }
   const float2 *P = reinterpret_cast<const float2 *>(Ppart);
@@ -899,7 +912,7 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
       gv[c][lane] = ms_row && c < a.C ? c2{g.x * e.x + g.y * e.y, g.y * e.x - g.x * e.y}
                                       : c2{0.f, 0.f};
     }
-    if (ms_row && a.grad_phi) a.grad_phi[k] = -dph;
+    if (ms_row && a.grad_phi) a.grad_phi[k] = bad ? obj_nan() : -dph;
   }
   if (!a.grad_W) return;
   __syncthreads();
@@ -942,7 +955,8 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
     }
     if (lane == 0) {
       const float2 g = __ldcg(reinterpret_cast<const float2 *>(GU) + (size_t)c * K + M + s2);
-      reinterpret_cast<float2 *>(a.grad_W)[i] = make_float2(g.x + acc.x, g.y + acc.y);
+      reinterpret_cast<float2 *>(a.grad_W)[i] =
+          bad ? make_float2(obj_nan(), obj_nan()) : make_float2(g.x + acc.x, g.y + acc.y);
     }
   }
   if (threadIdx.x == 0) *counter = 0u;  // ready for the next call
@@ -969,7 +983,10 @@ int cbucket(int C) {
   return b;
 }
 
-constexpr int kTargetBlocks = 152 * 8;
+// CTAs the CUDA-core split path aims for: a work split that fills a device
+// of this size (8 per SM on a 152-SM GB300) and that fixes the scratch
+// layout, so it is a constant rather than a device query
+constexpr int kTargetBlocks = 1216;
 
 struct Split {
   int K, kspl, kper, rspl, rper, nb_epi;
@@ -1004,7 +1021,8 @@ cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *U, float *Yp
     k_epilogue_wide<(CB >= 8 ? CB : 8)><<<(a.R + 31) / 32, 256, 0, st>>>(a, sp.kspl, Ypart, G1,
                                                                         G2, part, counter, scal);
   else
-    k_epilogue<CB><<<sp.nb_epi, 128, 0, st>>>(a, sp.kspl, Ypart, G1, G2, part, counter, scal);
+    k_epilogue<CB><<<sp.nb_epi, 128, 0, st>>>(a, sp.kspl, Ypart, G1, G2, part, counter, scal,
+                                              nullptr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (a.grad_Y) {
@@ -1119,7 +1137,15 @@ __global__ void __launch_bounds__(256, 2)
       abort_flag = 1;
     }
     __syncthreads();
-    if (abort_flag) break;
+    if (abort_flag) {
+      // before the CTA exits, let the copies it issued land (bounded again):
+      // this tile's and, if it was issued, the next tile's in the other stage
+      if (t == 0) {
+        mbar_wait_bounded(&full[stg], (it >> 1) & 1);
+        if (tile + (int)gridDim.x < ntiles) mbar_wait_bounded(&full[stg ^ 1], ((it + 1) >> 1) & 1);
+      }
+      break;
+    }
     const float2 *T = reinterpret_cast<const float2 *>(base + (size_t)stg * stage_bytes);
     // (A) Y for the tile's columns; lanes with equal col are TR apart
     c2 y[CB];
@@ -1278,16 +1304,7 @@ struct StreamPlan {
   size_t smem = 0;
 };
 
-int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 152;
-  }
-  return n;
-}
+int sm_count() { return ams_device_sms(); }
 
 // the single-pass path needs the whole [H_r; H_d] column tile in shared memory
 StreamPlan stream_plan(int S, int M, int R, int C, bool grad_y) {
@@ -1324,12 +1341,10 @@ cudaError_t launch_stream_t(const ObjArgs &a, const StreamPlan &pl, const CUtens
                             const CUtensorMap &md, int M, const float *U, float *Ppart,
                             double *lpart, unsigned *err, cudaStream_t st) {
   auto kfn = k_obj_stream<CB, TR, KPT>;
-  static size_t set_bytes = 0;
-  if (set_bytes < pl.smem) {
-    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)pl.smem);
+  static size_t set_bytes[AMS_MAX_DEVICES] = {0};
+  {
+    cudaError_t e = ams_set_smem_atleast(set_bytes, kfn, pl.smem);
     if (e != cudaSuccess) return e;
-    set_bytes = pl.smem;
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(pl.grid);
@@ -1362,7 +1377,7 @@ cudaError_t launch_stream_k(const ObjArgs &a, const StreamPlan &pl, const CUtens
 template <int CB>
 cudaError_t stream_tail(const ObjArgs &a, int M, int nparts, const float *U, const float *Pp,
                         const double *lp, float *GU, float *dwp, unsigned *counter,
-                        cudaStream_t st);
+                        const unsigned *err, cudaStream_t st);
 
 template <int CB>
 cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, float *Ppart,
@@ -1384,16 +1399,16 @@ cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, 
     default: e = launch_stream_k<CB, 2>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
   }
   if (e != cudaSuccess) return e;
-  return stream_tail<CB>(a, M, pl.grid, U, Ppart, lpart, GU, dwp, counter, st);
+  return stream_tail<CB>(a, M, pl.grid, U, Ppart, lpart, GU, dwp, counter, err, st);
 }
 
 // after a streaming kernel: G_U, dphi and the dL/dW parts, then dL/dW
 template <int CB>
 cudaError_t stream_tail(const ObjArgs &a, int M, int nparts, const float *U, const float *Pp,
                         const double *lp, float *GU, float *dwp, unsigned *counter,
-                        cudaStream_t st) {
+                        const unsigned *err, cudaStream_t st) {
   const int K = M + a.S, nblk = (K + 31) / 32;
-  k_stream_tail<CB><<<nblk, 1024, 0, st>>>(a, M, nparts, Pp, lp, U, GU, dwp, counter);
+  k_stream_tail<CB><<<nblk, 1024, 0, st>>>(a, M, nparts, Pp, lp, U, GU, dwp, counter, err);
   return cudaGetLastError();
 }
 
@@ -1486,7 +1501,15 @@ __global__ void __launch_bounds__(256)
       abort_flag = 1;
     }
     __syncthreads();
-    if (abort_flag) break;
+    if (abort_flag) {
+      // before the CTA exits, let the copies it issued land (bounded again):
+      // this tile's and, if it was issued, the next tile's in the other stage
+      if (t == 0) {
+        mbar_wait_bounded(&full[stg], (it >> 1) & 1);
+        if (tile + (int)gridDim.x < ntiles) mbar_wait_bounded(&full[stg ^ 1], ((it + 1) >> 1) & 1);
+      }
+      break;
+    }
     const float2 *T = reinterpret_cast<const float2 *>(base + (size_t)stg * stage_bytes);
     // (A) Y of column acol over this warp's runs of k
     {
@@ -1723,7 +1746,7 @@ __global__ void __launch_bounds__(128, 1)
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], done;
   __shared__ uint32_t tmem_slot;
-  __shared__ int abort_flag;
+  __shared__ int abort_flag, n_issued, n_used;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
   const int kb0 = blockIdx.z * kb_per;
@@ -1732,6 +1755,8 @@ __global__ void __launch_bounds__(128, 1)
     for (int s = 0; s < STAGES; s++) { tc::mbar_init(&full[s], 1); tc::mbar_init(&empty[s], 1); }
     tc::mbar_init(&done, 1);
     abort_flag = 0;
+    n_issued = 0;
+    n_used = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) tc::tmem_alloc(&tmem_slot, (uint32_t)BN);
@@ -1741,7 +1766,8 @@ __global__ void __launch_bounds__(128, 1)
   const uint32_t tmem = tmem_slot;
 
   if (warp == 0 && lane == 0) {
-    for (int kb = 0; kb < nk; kb++) {
+    int kb = 0;
+    for (; kb < nk; kb++) {
       const int s = kb % STAGES;
       if (kb >= STAGES && !tc::mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1)) {
         abort_flag = 1;
@@ -1757,9 +1783,11 @@ __global__ void __launch_bounds__(128, 1)
       tc::tma_load_2d(sp + 2 * A_BYTES, &tbh, x, n0, &full[s]);
       tc::tma_load_2d(sp + 2 * A_BYTES + B_BYTES, &tbl, x, n0, &full[s]);
     }
+    n_issued = kb;
   } else if (warp == 1 && lane == 0) {
     constexpr uint32_t idesc = tc::idesc_bf16(BM, BN);
-    for (int kb = 0; kb < nk; kb++) {
+    int kb = 0;
+    for (; kb < nk; kb++) {
       const int s = kb % STAGES;
       if (!tc::mbar_wait(&full[s], (kb / STAGES) & 1)) {
         abort_flag = 1;
@@ -1779,6 +1807,7 @@ __global__ void __launch_bounds__(128, 1)
       }
       tc::umma_commit(&empty[s]);
     }
+    n_used = kb;
     tc::umma_commit(&done);
   }
   __syncwarp();
@@ -1786,6 +1815,10 @@ __global__ void __launch_bounds__(128, 1)
   if (!have && lane == 0) atomicOr(err, 4u);
   // block-uniform: tcgen05.ld and the shuffles below are warp-collective
   const bool drain = __syncthreads_and(have ? 1 : 0) && !abort_flag;
+  // after an abort, the tiles issued but never consumed land before the CTA
+  // exits (each stage holds at most one of them; bounded waits again)
+  if (abort_flag && tid == 0)
+    for (int kb = n_used; kb < n_issued; kb++) tc::mbar_wait(&full[kb % STAGES], (kb / STAGES) & 1);
   tc::fence_after();
   if (drain) {
     const int row = warp * 32 + lane;
@@ -1829,6 +1862,25 @@ void pick_split(int ntiles, int nkb, int sms, int &ks, int &kper) {
 }
 
 }  // namespace
+
+namespace {
+std::atomic<int> g_inject_timeouts{0};
+}  // namespace
+
+// Start of a call on a path with bounded waits: its wait-timeout word is
+// cleared, so the word reports this call only.  An injected timeout (test
+// hook of the error path) sets it right away, as a wait that ran out would.
+cudaError_t obj_begin_call(unsigned *err, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(err, 0, 4, st);
+  if (e != cudaSuccess) return e;
+  int n = g_inject_timeouts.load();
+  while (n > 0 && !g_inject_timeouts.compare_exchange_weak(n, n - 1)) {
+  }
+  if (n > 0) e = cudaMemsetAsync(err, 1, 1, st);
+  return e;
+}
+
+void obj_inject_timeouts(int calls) { g_inject_timeouts.store(calls > 0 ? calls : 0); }
 
 ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C) {
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -1875,6 +1927,8 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
     double *lp = reinterpret_cast<double *>(scratch + L.lp);
     unsigned *err = reinterpret_cast<unsigned *>(scratch + L.inv + 48);
     float *GUs = reinterpret_cast<float *>(scratch + L.GUs);
+    cudaError_t e = obj_begin_call(err, st);
+    if (e != cudaSuccess) return e;
     if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Um, Pp, lp, GUs, gw, err, counter + 2, st);
     return run_stream<2>(a, pl, M, Um, Pp, lp, GUs, gw, err, counter + 2, st);
   }
@@ -1957,12 +2011,10 @@ template <int CB, int TR, int KPT>
 cudaError_t launch_stream_ht(ObjTcPlan *p, const ObjArgs &a, const float *U, float *Pp,
                              double *lp, unsigned *err, cudaStream_t st) {
   auto kfn = k_obj_stream_t<CB, TR, KPT>;
-  static size_t set_bytes = 0;
-  if (set_bytes < p->tSmem) {
-    cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)p->tSmem);
+  static size_t set_bytes[AMS_MAX_DEVICES] = {0};
+  {
+    cudaError_t e = ams_set_smem_atleast(set_bytes, kfn, p->tSmem);
     if (e != cudaSuccess) return e;
-    set_bytes = p->tSmem;
   }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(p->tGrid);
@@ -2001,9 +2053,10 @@ cudaError_t run_plan_stream(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st) {
   char *ctl = p->mem + p->oCtl;
   unsigned *counter = reinterpret_cast<unsigned *>(ctl + 40);
   unsigned *err = reinterpret_cast<unsigned *>(ctl + 48);
+  cudaError_t e = obj_begin_call(err, st);
+  if (e != cudaSuccess) return e;
   const long long n = (long long)M * a.C * 8;
   k_prep_wide<<<(int)((n + 255) / 256), 256, 0, st>>>(a, M, U);
-  cudaError_t e;
   switch (p->tTR) {
     case 8: e = launch_stream_ht_k<CB, 8>(p, a, U, Pp, lp, err, st); break;
     case 4: e = launch_stream_ht_k<CB, 4>(p, a, U, Pp, lp, err, st); break;
@@ -2011,7 +2064,7 @@ cudaError_t run_plan_stream(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st) {
   }
   if (e != cudaSuccess) return e;
   return stream_tail<CB>(a, M, p->tGrid, U, Pp, lp, gw, reinterpret_cast<float *>(p->mem + p->oDw),
-                         counter, st);
+                         counter, err, st);
 }
 }  // namespace
 
@@ -2074,13 +2127,9 @@ cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr
       tc::make_map_bf16(&p->m_agh, p->ag_hi, p->Mp, p->K2p, tcg::BM) &&
       tc::make_map_bf16(&p->m_agl, p->ag_lo, p->Mp, p->K2p, tcg::BM);
   if (!ok) { cudaFree(p->mem); delete p; return cudaErrorInvalidValue; }
-  static bool attr = false;
-  if (!attr) {
-    e = cudaFuncSetAttribute(k_cgemm3, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)tcg::SMEM);
-    if (e != cudaSuccess) { cudaFree(p->mem); delete p; return e; }
-    attr = true;
-  }
+  static size_t attr[AMS_MAX_DEVICES] = {0};
+  e = ams_set_smem_atleast(attr, k_cgemm3, tcg::SMEM);
+  if (e != cudaSuccess) { cudaFree(p->mem); delete p; return e; }
   // the A operands (rows beyond 2 C stay zero) and the control block
   e = cudaMemsetAsync(p->mem + oay, 0, o - oay, st);
   if (e == cudaSuccess) {
@@ -2094,6 +2143,10 @@ cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr
   if (e != cudaSuccess) { cudaFree(p->mem); delete p; return e; }
   *out = p;
   return cudaSuccess;
+}
+
+const unsigned *obj_tc_plan_status_word(const ObjTcPlan *p) {
+  return p ? reinterpret_cast<const unsigned *>(p->mem + p->oCtl + 48) : nullptr;
 }
 
 size_t obj_tc_plan_bytes(const ObjTcPlan *p) { return p ? p->bytes : 0; }
@@ -2118,6 +2171,10 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
   float *scal = reinterpret_cast<float *>(ctl);
   unsigned *counter = reinterpret_cast<unsigned *>(ctl + 32);
   unsigned *err = reinterpret_cast<unsigned *>(ctl + 48);
+  {
+    cudaError_t e0 = obj_begin_call(err, st);
+    if (e0 != cudaSuccess) return e0;
+  }
   k_prep<<<dim3((M + 127) / 128, C), 128, 0, st>>>(a, M, U);
   const long long nay = (long long)C * (p->Kp / 2);
   k_tc_make_ay<<<(unsigned)((nay + 255) / 256), 256, 0, st>>>(U, a.W, C, M, p->S, p->Kp,
@@ -2131,7 +2188,7 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
     float *maxr = G1;  // G1 / G2 are not needed on this branch: per-Rx max and argmax
     int *argr = reinterpret_cast<int *>(G2 ? G2 : G1 + R);
     const int nb = (R + 31) / 32;
-    k_tc_epi_a<CW><<<nb, 256, 0, st>>>(a, p->ksy, Ypart, maxr, argr, part, counter, scal);
+    k_tc_epi_a<CW><<<nb, 256, 0, st>>>(a, p->ksy, Ypart, maxr, argr, part, counter, scal, err);
     if (need_g || a.grad_Y) {
       // with no gradient wanted the A operand is still written (harmless)
       const int nbb = std::max(nb, (p->K2p / 2 + 31) / 32);
@@ -2140,7 +2197,7 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
     }
   } else {
     k_epilogue<CB><<<(R + 127) / 128, 128, 0, st>>>(a, p->ksy, Ypart, G1, G2, part, counter,
-                                                    scal);
+                                                    scal, err);
     if (a.grad_Y) {
       const long long n = (long long)C * R;
       k_grad_y<<<(int)((n + 255) / 256), 256, 0, st>>>(G1, G2, scal, n, a.grad_Y);
@@ -2160,12 +2217,13 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
   float *GU = reinterpret_cast<float *>(p->mem + p->oGUs);
   const long long ngu = (long long)C * p->K;
   k_gu_reduce<<<(unsigned)((ngu + 255) / 256), 256, 0, st>>>(GUp, p->ksg, ngu, GU);
-  if (a.grad_phi) k_tc_dphi<<<(M + 31) / 32, 256, 0, st>>>(GU, U, C, M, p->K, a.grad_phi);
+  if (a.grad_phi) k_tc_dphi<<<(M + 31) / 32, 256, 0, st>>>(GU, U, C, M, p->K, a.grad_phi, err);
   if (a.grad_W) {
     float *dwp = reinterpret_cast<float *>(p->mem + p->oDw);
     k_tc_dw_part<<<dim3(C, kDwParts), 128, 0, st>>>(GU, p->Ha, a.phi, a.max_phase, p->S, M,
                                                     p->K, dwp);
-    k_tc_dw_sum<<<(C * p->S + 127) / 128, 128, 0, st>>>(GU, dwp, C, p->S, M, p->K, a.grad_W);
+    k_tc_dw_sum<<<(C * p->S + 127) / 128, 128, 0, st>>>(GU, dwp, C, p->S, M, p->K, a.grad_W,
+                                                        err);
   }
   return cudaGetLastError();
 }

@@ -30,6 +30,13 @@ ObjScratchLayout obj_scratch_layout(int S, int M, int R, int C);
 cudaError_t obj_run(const ObjArgs &a, char *scratch, cudaStream_t st);
 cudaError_t coverage_db_run(const float *H, int S, int R, float threshold, float offset,
                             float *out, cudaStream_t st);
+// Wait-timeout word: the kernels with bounded mbarrier waits set the word at
+// control-block offset 48 when a wait runs out; every call on such a path
+// clears it first (obj_begin_call), and the call's outputs are then NaN.
+cudaError_t obj_begin_call(unsigned *err, cudaStream_t st);
+// test hook: the next `calls` calls on paths with bounded waits behave as if
+// one of their waits had run out
+void obj_inject_timeouts(int calls);
 // scratch of the allocation-free entry point (objective.cu); the first call
 // on a device looks up the array's device address
 cudaError_t obj_noalloc_scratch(char **out);
@@ -46,5 +53,7 @@ cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr
                                int R, int Cmax, cudaStream_t st, ObjTcPlan **out);
 cudaError_t obj_tc_run(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st);
 size_t obj_tc_plan_bytes(const ObjTcPlan *p);
+// device address of the plan's wait-timeout word
+const unsigned *obj_tc_plan_status_word(const ObjTcPlan *p);
 bool obj_tc_plan_streams(const ObjTcPlan *p);
 void obj_tc_plan_destroy(ObjTcPlan *p);

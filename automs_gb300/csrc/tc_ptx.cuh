@@ -8,6 +8,8 @@
 
 #include <cstdint>
 
+#include "ams_common.cuh"
+
 namespace tc {
 
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per mbarrier wait

@@ -1006,7 +1006,7 @@ __global__ void k_export(TraceDev P, int32_t *out, unsigned long long *n_out) {
 
 int grid_for(long long n, int block) {
   long long b = (n + block - 1) / block;
-  const long long cap = 152LL * 16;
+  const long long cap = (long long)ams_device_sms() * 16;
   if (b > cap) b = cap;
   if (b < 1) b = 1;
   return (int)b;
@@ -1018,22 +1018,16 @@ cudaError_t trace_stage1(const TraceDev &P, cudaStream_t st) {
   // persistent: as many CTAs as are resident at once (lanes fetch launch
   // indices from ctr[10], zeroed with the other counters)
   long long n = (long long)P.launch_x * P.launch_y;
-  static int per_sm[64] = {0};
-  static int n_sm[64] = {0};
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  static int per_sm[AMS_MAX_DEVICES] = {0};
+  const int dev = ams_current_device();
+  if (dev < 0) return cudaErrorInvalidDevice;
   if (per_sm[dev] == 0) {
-    int b = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_stage1, 128, 0);
+    int b = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_stage1, 128, 0);
     if (e != cudaSuccess) return e;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return e;
-    n_sm[dev] = sms > 0 ? sms : 1;
     per_sm[dev] = b > 0 ? b : 1;
   }
-  long long blocks = (long long)per_sm[dev] * n_sm[dev];
+  long long blocks = (long long)per_sm[dev] * ams_device_sms();
   const long long need = (n + 127) / 128;
   if (blocks > need) blocks = need;
   if (blocks < 1) blocks = 1;
@@ -1051,7 +1045,7 @@ cudaError_t trace_stage2(const TraceDev &P, unsigned long long n_tasks, cudaStre
   if (n_tasks == 0) return cudaSuccess;
   unsigned long long rays = n_tasks * (unsigned long long)(P.gs * P.gs) * P.n_src;
   long long blocks = (long long)((rays + 255) / 256);
-  const long long cap = 152LL * 8 * 16;
+  const long long cap = (long long)ams_device_sms() * 8 * 16;
   if (blocks > cap) blocks = cap;
   k_stage2<<<(int)blocks, 256, 0, st>>>(P, n_tasks);
   return cudaGetLastError();

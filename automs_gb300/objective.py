@@ -133,6 +133,14 @@ def capacity_objective(W, H_d, H_a=None, H_r=None, phi=None, max_phase=2 * math.
     return (loss, recv) if return_recv else loss
 
 
+def check_status(plan=None):
+    """Raise AmsError if a bounded wait of the last objective call ran out
+    (its outputs are then NaN): the last call on `plan`, or with plan=None the
+    last direct call on the current device.  Synchronises the stream."""
+    h = plan._h if plan is not None else None
+    call("ams_objective_status", h if h is not None else C.c_void_p(0), _stream())
+
+
 def mean_capacity(wvec, H_d, H_a=None, H_r=None, phi=None):
     """-mean over Rx of log2(1 + |y|^2 / N0) with one complex weight vector:
     the reference loss with C = 1, w = 1/R and no dropout."""
@@ -188,6 +196,12 @@ class Model(nn.Module):
         for i in range(len(self.ms_list)):
             self.ms_theta[i] = self.ms_theta[i] % self.ms_list[i].max_phase
         self.forward()
+
+    def check_status(self):
+        """Raise if a bounded wait of the last evaluation ran out."""
+        for plan in self._plans.values():
+            check_status(plan)
+        check_status()
 
     def pick_channel(self, choose_new=False):
         if self.global_random:
@@ -278,3 +292,4 @@ def optimize_model(model: Model, lr: float = 0.3, step: int = 200, progress=Fals
         for t, b in zip(model.ms_theta, best_ms):
             t.copy_(b)
     model.forward()
+    model.check_status()

@@ -173,7 +173,6 @@ ams_status ams_objective_fwd_bwd_noalloc(
     const uint8_t *drop, float *loss, float *grad_W, float *grad_phi,
     float *grad_Y, float *recv_amp, void *stream, char *errbuf, size_t errlen);
 
-/* Received amplitude |Y| [C,R] of the same model (forward only). */
 /* Evaluation plan of ams_objective_fwd_bwd for a fixed channel set (one
  * metasurface hop) evaluated many times -- the optimizer loop of
  * optimize_model (go.py:296-336), with the reference's code_num codes or
@@ -208,6 +207,27 @@ ams_status ams_objective_plan_fwd_bwd(ams_objective_plan *plan,
 unsigned long long ams_objective_plan_bytes(const ams_objective_plan *plan);
 void ams_objective_plan_destroy(ams_objective_plan *plan);
 
+/* Wait-timeout report of the objective.  The streaming and tensor-core
+ * kernels wait on TMA copies with a 2 s limit per wait; when a wait runs out
+ * the kernel drains its copies in flight, the call's outputs (loss,
+ * gradients) are written as NaN, and this call reports it: it synchronises
+ * `stream` and returns AMS_ERR_INTERNAL (message in errbuf) if a wait of the
+ * last call on `plan` -- or, with plan == NULL, of the last
+ * ams_objective_fwd_bwd / ams_objective_fwd_bwd_noalloc call on the current
+ * device -- ran out, AMS_OK otherwise.  Each call clears its own report when
+ * it starts.  No counterpart in the reference (whose op returns void,
+ * optixPathTracer.cpp:858-860). */
+ams_status ams_objective_status(const ams_objective_plan *plan, void *stream,
+                                char *errbuf, size_t errlen);
+
+/* Fault injection for tests of the error path: the next `calls` objective
+ * calls that take a path with bounded waits (streaming or tensor-core
+ * kernels) report one of their waits as run out, exactly as a TMA copy that
+ * did not arrive in time would, without waiting less or touching the GPU's
+ * state.  0 cancels.  Not for production use. */
+void ams_debug_inject_wait_timeout(int calls);
+
+/* Received amplitude |Y| [C,R] of the same model (forward only). */
 ams_status ams_objective_recv(const float *H_d, const float *H_a,
                               const float *H_r, const float *phi,
                               float max_phase, const float *W, int S, int M,

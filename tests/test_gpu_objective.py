@@ -285,3 +285,78 @@ def test_tensor_core_plan_errors(obj):
     with pytest.raises(AmsError):
         obj.capacity_objective(W, Hd, Ha, Hr, phi, plan=plan)
     plan.close()
+
+
+def test_tensor_core_plan_config3_shape_vs_oracle(obj):
+    """The 3xBF16 tensor-core plan at the full channel-set shape (S=16,
+    M=32x32, R=256x256, a 60-code codebook) against the FP64 oracle: loss
+    and |Y| to 1e-4 relative, gradients to 1e-3 of their scale; the measured
+    errors are printed."""
+    rng = np.random.Generator(np.random.PCG64(31))
+    S, M, R, C = 16, 1024, 65536, 60
+    ch = {"src_to_dst": cases._cn(rng, (S, R)), "src_to_ms{0}": cases._cn(rng, (S, M)),
+          "ms{0}_to_dst": cases._cn(rng, (M, R))}
+    c = dict(channels=ch, theta=rng.uniform(0, 2 * np.pi, size=(C, S)).astype(np.float32),
+             phi=[rng.uniform(0, 2 * np.pi, size=M).astype(np.float32)], n_ms=1, code_num=C,
+             w=1.0 / R, max_phase_deg=360.0)
+    ch, theta_np, A, drop, mp = _tc_inputs(c)
+    Hd, Ha, Hr = ch["src_to_dst"], ch["src_to_ms{0}"], ch["ms{0}_to_dst"]
+    phi = c["phi"][0]
+    loss_o, gth_o, gphi_o, ex = OO.objective(Hd, Ha, Hr, phi, theta_np, A, c["w"], drop, mp)
+    dHd, dHa, dHr = cuda(Hd), cuda(Ha), cuda(Hr)
+    plan = obj.ObjectivePlan(dHd, dHa, dHr, c_max=C)
+    theta = cuda(theta_np).requires_grad_(True)
+    W = cuda(A.astype(np.float32)) * torch.exp(-1j * theta)
+    ph = cuda(phi).requires_grad_(True)
+    loss, recv = obj.capacity_objective(W, dHd, dHa, dHr, ph, mp, c["w"], cuda(drop),
+                                        return_recv=True, plan=plan)
+    loss.backward()
+    obj.check_status(plan)
+    amp = recv.cpu().numpy()
+    g, gp = theta.grad.cpu().numpy(), ph.grad.cpu().numpy()
+    e_loss = abs(float(loss) - loss_o) / abs(loss_o)
+    e_amp = np.abs(amp - ex["amp"]).max() / np.abs(ex["amp"]).max()
+    e_th = np.abs(g - gth_o).max() / np.abs(gth_o).max()
+    e_ph = np.abs(gp - gphi_o).max() / np.abs(gphi_o).max()
+    print(f"3xBF16 at R=65536 C=60 vs FP64: loss {e_loss:.2e}, |Y| {e_amp:.2e}, "
+          f"dtheta {e_th:.2e}, dphi {e_ph:.2e}")
+    assert e_loss < 1e-4 and e_amp < 1e-4
+    assert e_th < 1e-3 and e_ph < 1e-3
+    plan.close()
+
+
+@pytest.mark.parametrize("path", ["direct", "stream_plan", "tensor_core_plan"])
+def test_wait_timeout_is_reported(obj, path):
+    """A bounded wait that runs out (injected on the host: the kernels wait
+    exactly as usual) makes the call's loss and gradients NaN and the status
+    call report it; the next call is clean and matches an undisturbed one."""
+    from automs_gb300._lib import AmsError, lib
+    rng = np.random.Generator(np.random.PCG64(41))
+    S, M, R = 16, 1024, 4096
+    C = 60 if path == "tensor_core_plan" else 1
+    Hd, Ha, Hr = (cuda(cases._cn(rng, sh)) for sh in ((S, R), (S, M), (M, R)))
+    W = torch.exp(-1j * cuda(rng.uniform(0, 2 * np.pi, size=(C, S)).astype(np.float32)))
+    phi = cuda(rng.uniform(0, 2 * np.pi, size=M).astype(np.float32))
+    plan = None if path == "direct" else obj.ObjectivePlan(Hd, Ha, Hr, c_max=C)
+
+    def run():
+        Wg = W.clone().requires_grad_(True)
+        pg = phi.clone().requires_grad_(True)
+        loss = obj.capacity_objective(Wg, Hd, Ha, Hr, pg, 2 * np.pi, 1.0 / R, plan=plan)
+        loss.backward()
+        return float(loss), Wg.grad.clone(), pg.grad.clone()
+    clean = run()
+    obj.check_status(plan)
+    lib().ams_debug_inject_wait_timeout(1)
+    bad = run()
+    assert np.isnan(bad[0])
+    assert torch.isnan(bad[1]).all() and torch.isnan(bad[2]).all()
+    with pytest.raises(AmsError) as ei:
+        obj.check_status(plan)
+    assert ei.value.status == 7
+    again = run()
+    obj.check_status(plan)
+    assert again[0] == clean[0]
+    assert torch.equal(again[1], clean[1]) and torch.equal(again[2], clean[2])
+    if plan is not None:
+        plan.close()
