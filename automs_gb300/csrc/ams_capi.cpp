@@ -391,8 +391,9 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     need += al(sizeof(float) * 6 * (size_t)n_src) + al(sizeof(float) * 6 * (size_t)n_dst);
     need += al(std::max(lbvh_scratch_bytes(n_src), lbvh_scratch_bytes(n_dst)));
     need += al(lbvh_output_bytes(n_src)) + al(lbvh_output_bytes(n_dst));
-    need += al(8 * (size_t)tab_size) + al(4 * (size_t)tab_size) + al(56 * (size_t)tab_size);
+    need += al(8 * (size_t)tab_size) + al(56 * (size_t)tab_size);
     need += 3 * al(4 * (size_t)ng * W);
+    need += al(4 * ((size_t)ng + 1)) + al(4 * (size_t)ng) + al(8 * ((size_t)ng + 1)) + al(4);
     need += al(16 * (size_t)n_src * n_dst);
     need += al(8 * 16) + al(4);
     need += 4096;
@@ -406,11 +407,14 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     char *rx_out = S->ws.take<char>(lbvh_output_bytes(n_dst));
     TraceDev P{};
     P.tab_h = S->ws.take<unsigned long long>(tab_size);
-    P.tab_chk = S->ws.take<unsigned>(tab_size);
     P.tab_key = S->ws.take<int32_t>(14 * (size_t)tab_size);
     P.T = S->ws.take<unsigned>((size_t)ng * W);
     P.N = S->ws.take<unsigned>((size_t)ng * W);
     P.S = S->ws.take<unsigned>((size_t)ng * W);
+    P.cell_off = S->ws.take<int>((size_t)ng + 1);
+    P.act_cells = S->ws.take<int>((size_t)ng);
+    P.item_off = S->ws.take<long long>((size_t)ng + 1);
+    P.n_act = S->ws.take<int>(1);
     P.acc = S->ws.take<unsigned long long>(2 * (size_t)n_src * n_dst);
     P.ctr = S->ws.take<unsigned long long>(16);
     P.err = S->ws.take<unsigned>(1);
@@ -443,7 +447,7 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     P.W = W;
 
     CK(cudaMemsetAsync(P.tab_h, 0, 8 * (size_t)tab_size, st));
-    CK(cudaMemsetAsync(P.tab_chk, 0, 4 * (size_t)tab_size, st));
+    CK(cudaMemsetAsync(P.tab_key, 0, 56 * (size_t)tab_size, st));  // 0 = word not written
     CK(cudaMemsetAsync(P.T, 0, 4 * (size_t)ng * W, st));
     CK(cudaMemsetAsync(P.S, 0, 4 * (size_t)ng * W, st));
     CK(cudaMemsetAsync(P.acc, 0, 16 * (size_t)n_src * n_dst, st));
@@ -481,14 +485,16 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     if (fwd_records > 0) {
       CK(cudaMemcpyAsync(P.N, P.T, 4 * (size_t)ng * W, cudaMemcpyDeviceToDevice, st));
       while (n_new > 0) {
-        if (S->tasks.cap < n_new * sizeof(int2)) {
+        if (S->tasks.cap < n_new * sizeof(int)) {
           CK(cudaStreamSynchronize(st));
-          CK(S->tasks.ensure(std::max<size_t>(n_new * sizeof(int2) * 2, 1 << 20)));
+          CK(S->tasks.ensure(std::max<size_t>(n_new * sizeof(int) * 2, 1 << 20)));
         }
-        P.tasks = reinterpret_cast<int2 *>(S->tasks.base);
-        P.task_cap = S->tasks.cap / sizeof(int2);
+        P.task_slot = reinterpret_cast<int *>(S->tasks.base);
+        P.task_cap = S->tasks.cap / sizeof(int);
+        P.kpi = trace_paths_per_item(P, n_new);
         CK(cudaMemsetAsync(P.ctr + 5, 0, 8, st));
         CK(cudaMemsetAsync(P.ctr + 7, 0, 8, st));
+        CK(cudaMemsetAsync(P.ctr + 11, 0, 8, st));
         CK(trace_make_tasks(P, P.N, st));
         CK(cudaEventRecord(S->k2[0], st));
         CK(trace_stage2(P, n_new, st));

@@ -387,52 +387,68 @@ __device__ __forceinline__ int32_t fbits(float f) {
   return b == (int32_t)0x80000000 ? 0 : b;  // -0 and +0 are one key
 }
 
-// Path-key hashes: word-wise FNV-1a (Fowler, Noll, Vo) in 64 and 32 bits
-// with different offsets and primes, each finished by an avalanche mixer.
-// The 64-bit one places the key; the 32-bit one detects collisions.
+// Path-key hash: word-wise FNV-1a (Fowler, Noll, Vo) in 64 bits, finished
+// by an avalanche mixer; it places the key in the open-addressed table.
 __device__ __forceinline__ uint64_t key_hash64(const int32_t *k) {
   uint64_t h = 0xcbf29ce484222325ull;
 #pragma unroll
   for (int i = 0; i < 14; i++) h = (h ^ (uint64_t)(uint32_t)k[i]) * 0x100000001b3ull;
   return mix64(h);
 }
-__device__ __forceinline__ uint32_t key_hash32(const int32_t *k) {
-  uint32_t h = 0x811c9dc5u;
-#pragma unroll
-  for (int i = 0; i < 14; i++) h = (h ^ (uint32_t)k[i]) * 0x01000193u;
-  return mix32(h);
-}
 
 // OR a bit into a bitmap word (a reduction: the thread does not wait)
 __device__ __forceinline__ void set_bit(unsigned *word, unsigned bit) { atomicOr(word, bit); }
 
-// claim or find the slot of a path key; returns -1 when the table is full
+// Key words are stored with the sign bit flipped.  A key never holds
+// 0x80000000 (-0.0 is canonicalised to +0, and the hit count and reflect
+// mask are small non-negative integers), so a stored word is never 0, and a
+// 0 read back from a slot is a word its claiming thread has not written yet.
+#define AMS_KEY_FLIP 0x80000000u
+__device__ __forceinline__ int32_t key_word(const int32_t *slot_key, int i) {
+  return (int32_t)((uint32_t)__ldg(slot_key + i) ^ AMS_KEY_FLIP);
+}
+
+// Claim or find the slot of a path key; returns -1 when the table is full.
+// The 64-bit hash picks the first probe; a slot belongs to the key whose
+// 14 words are stored in it.  One batch of loads reads a slot's hash and
+// words: a slot with the same hash whose words are all written (non-zero)
+// and equal is the key's slot; one whose words are still being written is
+// re-read until they are (a few instructions of the claiming thread; the
+// wait is bounded); a slot holding other words is passed over.  So two
+// distinct keys never share a slot, and a key never takes two.
 __device__ int path_insert(const TraceDev &P, const int32_t *key) {
   const uint64_t h = key_hash64(key) | 1ull;
-  const uint32_t c = key_hash32(key) | 1u;
+  uint32_t enc[14];
+#pragma unroll
+  for (int i = 0; i < 14; i++) enc[i] = (uint32_t)key[i] ^ AMS_KEY_FLIP;
   uint32_t slot = (uint32_t)h & P.tab_mask;
   for (uint32_t probe = 0; probe <= P.tab_mask; probe++) {
-    // most records repeat a key already in the table: look before the CAS
-    // (both words of the slot in one round trip)
     unsigned long long old = __ldcg(P.tab_h + slot);
-    const unsigned chk = __ldcg(P.tab_chk + slot);
-    if (old == (unsigned long long)h && chk == c) return (int)slot;
+    uint32_t *sk = reinterpret_cast<uint32_t *>(P.tab_key) + (size_t)slot * 14;
     if (old == 0ull) old = atomicCAS(P.tab_h + slot, 0ull, (unsigned long long)h);
     if (old == 0ull) {
-      int32_t *dst = P.tab_key + (size_t)slot * 14;
 #pragma unroll
-      for (int i = 0; i < 14; i++) dst[i] = key[i];
-      unsigned o = atomicCAS(P.tab_chk + slot, 0u, c);
-      if (o != 0u && o != c) atomicOr(P.err, AMS_DERR_HASH);
+      for (int i = 0; i < 14; i++) __stcg(sk + i, enc[i]);
       unsigned long long occ = atomicAdd(P.ctr + 2, 1ull);
       if (occ >= P.tab_limit) atomicOr(P.err, AMS_DERR_PATH_TABLE);
       return (int)slot;
     }
     if (old == (unsigned long long)h) {
-      unsigned o = __ldcg(P.tab_chk + slot);
-      if (o == 0u) o = atomicCAS(P.tab_chk + slot, 0u, c);
-      if (o != 0u && o != c) atomicOr(P.err, AMS_DERR_HASH);
-      return (int)slot;
+      for (int spin = 0;; spin++) {
+        uint32_t w[14];
+        bool full = true, same = true;
+#pragma unroll
+        for (int i = 0; i < 14; i++) w[i] = __ldcg(sk + i);
+#pragma unroll
+        for (int i = 0; i < 14; i++) {
+          full &= w[i] != 0u;
+          same &= w[i] == enc[i];
+        }
+        if (same) return (int)slot;
+        if (full) break;  // another key with this hash: probe on
+        if (spin > (1 << 22)) { atomicOr(P.err, AMS_DERR_HASH); return -1; }
+        __nanosleep(32);
+      }
     }
     slot = (slot + 1u) & P.tab_mask;
   }
@@ -449,20 +465,35 @@ __device__ __forceinline__ void scene_tri(const TraceDev &P, int prim, af3 &v0, 
 }
 
 // ---------------------------------------------------------------- stage 1
+// A branch slot whose ray waits while an earlier-indexed one is traced (the
+// reference's 32-entry PRD stack, optixPathTracer.cu:152-190).  Its
+// remaining levels follow from the index: a reflection spawned at hit count
+// hc sets bit hc - 1 as the slot's highest bit and keeps L + 1 - hc levels.
 struct Slot {
   af3 o, d;
   Mat34 M;
-  int ttl;
 };
 
-// image matrix of a branch slot; slot 0 is the primary ray (identity)
-__device__ __forceinline__ Mat34 slot_matrix(const Slot *slots, int i) {
-  if (i != 0) return slots[i].M;
-  Mat34 I;
+__device__ __forceinline__ int slot_ttl(int L, int j) { return L - (31 - __clz(j)); }
+
+// Image matrix of the lane's current ray: slot 0 (the primary ray) is the
+// identity and is never stored; any other slot's matrix lives in shared
+// memory, entry k of lane t at cm[k * blockDim.x + t] (no bank conflicts).
+struct CurMatrix {
+  float *cm;  // this CTA's [12][blockDim.x] array
+  __device__ __forceinline__ Mat34 get(int cur) const {
+    Mat34 M;
 #pragma unroll
-  for (int k = 0; k < 12; k++) I.m[k] = (k == 0 || k == 5 || k == 10) ? 1.0f : 0.0f;
-  return I;
-}
+    for (int k = 0; k < 12; k++)
+      M.m[k] = cur == 0 ? ((k == 0 || k == 5 || k == 10) ? 1.0f : 0.0f)
+                        : cm[k * blockDim.x + threadIdx.x];
+    return M;
+  }
+  __device__ __forceinline__ void set(const Mat34 &M) const {
+#pragma unroll
+    for (int k = 0; k < 12; k++) cm[k * blockDim.x + threadIdx.x] = M.m[k];
+  }
+};
 
 
 
@@ -534,7 +565,8 @@ struct S1Ray {
 // the hit of the finished query (stage-1 closest-hit program,
 // optixPathTracer.cu:285-331)
 __device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, Slot *slots,
-                                    int *rec, unsigned long long &my_records) {
+                                    const CurMatrix &cm, int *rec,
+                                    unsigned long long &my_records) {
   const int L = P.L;
   if (q.best.inst == 3) { w.ttl = 0; return; }
   const af3 d = q.r.d;
@@ -552,16 +584,27 @@ __device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, 
     w.ttl--;
     int hc = L + 1 - w.ttl;
     int j = w.cur | (1 << (hc - 1));
-    Slot &c = slots[j];
-    c.ttl = w.ttl;
-    c.o = o;
-    c.d = sub3(d, scl3(N, 2.0f * dot3(d, N)));
-    c.M = slot_matrix(slots, w.cur);
-    af3 V = sub3(v0, image_of(c.M, w.spos));
+    Mat34 M = cm.get(w.cur);
+    af3 V = sub3(v0, image_of(M, w.spos));
     af3 Nimg = faceforward3(N0, V, N0);
-    image_update(c.M, Nimg, v0);
-    w.pending |= 1u << j;
-    if (!pen) w.ttl = 0;
+    image_update(M, Nimg, v0);
+    const af3 dr = sub3(d, scl3(N, 2.0f * dot3(d, N)));
+    if (!pen && (w.pending & ((1u << j) - 1u)) == 0u) {
+      // the current ray stops and the new slot is the lowest pending one, so
+      // it is the next to be traced: continue with it at once, without
+      // storing it (always the case when no material is penetrable)
+      w.cur = j;
+      w.guard = 0;
+      q.r.d = dr;
+      cm.set(M);
+    } else {
+      Slot &c = slots[j];
+      c.o = o;
+      c.d = dr;
+      c.M = M;
+      w.pending |= 1u << j;
+      if (!pen) w.ttl = 0;
+    }
   } else if (q.best.inst == 2) {
     if (w.res_cnt < P.reserve) {
       int d0 = q.best.prim / P.n1_dst, d1 = q.best.prim % P.n1_dst;
@@ -576,7 +619,9 @@ __device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, 
         if (w.key_cur != w.cur || w.key_ttl != w.ttl) {
           int32_t key[14];
 #pragma unroll
-          for (int k = 0; k < 12; k++) key[k] = fbits(slot_matrix(slots, w.cur).m[k]);
+          const Mat34 M = cm.get(w.cur);
+#pragma unroll
+          for (int k = 0; k < 12; k++) key[k] = fbits(M.m[k]);
           key[12] = hc;
           key[13] = w.cur;
           slot = path_insert(P, key);
@@ -596,8 +641,8 @@ __device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, 
 // next query of the lane: the current slot's next segment, the next pending
 // slot, the next sub-launch, or the next launch index.  Returns false when
 // no launch index is left.
-__device__ __forceinline__ bool s1_next(const TraceDev &P, S1Query &q, S1Ray &w, Slot *slots,
-                                       long long n_fetch, long long tiles_y,
+__device__ __forceinline__ bool s1_next(const TraceDev &P, S1Query &q, S1Ray &w, const Slot *slots,
+                                       const CurMatrix &cm, long long n_fetch, long long tiles_y,
                                        unsigned long long &my_capped) {
   while (true) {
     if (w.ttl > 0) {
@@ -617,7 +662,8 @@ __device__ __forceinline__ bool s1_next(const TraceDev &P, S1Query &q, S1Ray &w,
       w.pending &= w.pending - 1u;
       q.r.o = slots[w.cur].o;
       q.r.d = slots[w.cur].d;
-      w.ttl = slots[w.cur].ttl;
+      cm.set(slots[w.cur].M);
+      w.ttl = slot_ttl(P.L, w.cur);
       w.guard = 0;
       continue;
     }
@@ -629,7 +675,7 @@ __device__ __forceinline__ bool s1_next(const TraceDev &P, S1Query &q, S1Ray &w,
       w.spos = ld3(P.src + 3 * src);
       // slot 0 (the primary ray) starts at once: origin and direction go
       // straight into the query, and its image matrix is the identity,
-      // which is never stored (slot_matrix)
+      // which is never stored (CurMatrix)
       q.r.o = w.spos;
       q.r.d = rand_dir(w.seed, (uint32_t)w.ix, (uint32_t)w.iy, P.launch_x, P.launch_y);
       w.cur = 0;
@@ -666,13 +712,18 @@ __device__ __forceinline__ bool s1_next(const TraceDev &P, S1Query &q, S1Ray &w,
   }
 }
 
-// 8 CTAs of 128 per SM (64 registers) measured fastest among 4 to 12
+// 8 CTAs of 128 per SM (64 registers) measured fastest among 4 to 12.
+// LMAX bounds max_reflection: 2^LMAX branch slots (slot indices hold one bit
+// per hit count below L).
+template <int LMAX>
 __global__ void __launch_bounds__(128, 8) k_stage1(TraceDev P) {
   const long long tiles_y = (P.launch_y + 7) / 8;
   const long long n_fetch = (long long)((P.launch_x + 3) / 4) * tiles_y * 32;
   unsigned long long my_records = 0, my_segs = 0, my_capped = 0;
+  __shared__ float s_curm[12 * 128];
+  const CurMatrix cm{s_curm};
   int rec[AMS_MAX_RESERVE];  // cell * 8 + hit_cnt of the records kept so far
-  Slot slots[32];
+  Slot slots[1 << LMAX];     // deferred branch slots
   int st_node[AMS_STACK];
   float st_t[AMS_STACK];
 
@@ -685,7 +736,7 @@ __global__ void __launch_bounds__(128, 8) k_stage1(TraceDev P) {
   q.Dq = mk3(0.f, 0.f, 1.f);
   q.best.t = AMS_TMAX; q.best.inst = 3; q.best.prim = 0x7fffffff;
   q.phase = PH_HIT; q.node = 0; q.sp = 0;
-  bool live = s1_next(P, q, w, slots, n_fetch, tiles_y, my_capped);
+  bool live = s1_next(P, q, w, slots, cm, n_fetch, tiles_y, my_capped);
 
   while (__any_sync(0xffffffffu, live)) {
     // ---- traversal: node visits until every lane's query has ended
@@ -757,8 +808,8 @@ __global__ void __launch_bounds__(128, 8) k_stage1(TraceDev P) {
     // ---- hits of the waiting lanes, then their next queries
     if (live && q.phase == PH_HIT) {
       my_segs++;
-      s1_hit(P, q, w, slots, rec, my_records);
-      live = s1_next(P, q, w, slots, n_fetch, tiles_y, my_capped);
+      s1_hit(P, q, w, slots, cm, rec, my_records);
+      live = s1_next(P, q, w, slots, cm, n_fetch, tiles_y, my_capped);
     }
   }
   // block-aggregated counters
@@ -776,174 +827,283 @@ __global__ void __launch_bounds__(128, 8) k_stage1(TraceDev P) {
 }
 
 // --------------------------------------------------------------- tasks
-// list the set bits of a [ng][W] bitmap as (cell, slot) tasks
-__global__ void k_make_tasks(TraceDev P, const unsigned *bits) {
-  const long long nwords = (long long)P.ng * P.W;
-  const long long stride = (long long)gridDim.x * blockDim.x;
+// The round's tasks, listed per cell: cell c's new paths are task_slot[
+// cell_off[c] .. cell_off[c + 1]) in increasing slot order; the cells with at
+// least one are act_cells[0 .. n_act), and active cell a owns the stage-2
+// items item_off[a] .. item_off[a + 1): ceil(paths / kpi) path chunks times
+// G groups of 32 (Rx, Tx) pairs.  A warp per cell counts, one CTA scans, a
+// warp per cell fills.
+__device__ __forceinline__ long long s2_groups(const TraceDev &P) {
+  return ((long long)P.gs * P.gs * P.n_src + 31) / 32;
+}
+
+__global__ void k_cell_counts(TraceDev P, const unsigned *bits) {
   const int lane = threadIdx.x & 31;
-  for (long long base = (long long)blockIdx.x * blockDim.x; base < nwords; base += stride) {
-    long long wi = base + threadIdx.x;
-    unsigned w = wi < nwords ? bits[wi] : 0u;
-    int cnt = __popc(w);
-    int incl = cnt;
-    for (int off = 1; off < 32; off <<= 1) {
-      int v = __shfl_up_sync(0xffffffffu, incl, off);
-      if (lane >= off) incl += v;
+  const int nwarp = (gridDim.x * blockDim.x) >> 5;
+  for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < P.ng; cell += nwarp) {
+    const unsigned *row = bits + (size_t)cell * P.W;
+    int c = 0;
+    for (int w = lane; w < P.W; w += 32) c += __popc(row[w]);
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) P.cell_off[cell] = c;
+  }
+}
+
+// exclusive scan of the counts in place (cell_off[ng] = total), the active
+// cell list with its item offsets; one CTA of 1024 threads
+__global__ void __launch_bounds__(1024) k_cell_scan(TraceDev P) {
+  __shared__ long long wsum[32], wits[32];
+  __shared__ int wact[32];
+  __shared__ long long carry_s, icarry_s;
+  __shared__ int act_s;
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const long long G = s2_groups(P);
+  if (t == 0) { carry_s = 0; icarry_s = 0; act_s = 0; }
+  __syncthreads();
+  for (int base = 0; base < P.ng; base += 1024) {
+    const int i = base + t;
+    const long long v = i < P.ng ? P.cell_off[i] : 0;
+    const long long it = (v + P.kpi - 1) / P.kpi * G;  // items of this cell
+    long long x = v, y = it;
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long x2 = __shfl_up_sync(0xffffffffu, x, o);
+      const long long y2 = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) { x += x2; y += y2; }
     }
-    int total = __shfl_sync(0xffffffffu, incl, 31);
-    unsigned long long start = 0;
-    if (lane == 31 && total) start = atomicAdd(P.ctr + 5, (unsigned long long)total);
-    start = __shfl_sync(0xffffffffu, start, 31);
-    if (!total) continue;
-    unsigned long long pos = start + (unsigned long long)(incl - cnt);
-    int cell = (int)(wi / P.W);
-    int wo = (int)(wi % P.W);
-    while (w) {
-      int b = __ffs(w) - 1;
-      w &= w - 1u;
-      if (pos < P.task_cap) P.tasks[pos] = make_int2(cell, wo * 32 + b);
-      else atomicOr(P.err, AMS_DERR_TASKS);
-      pos++;
+    const unsigned act = __ballot_sync(0xffffffffu, v > 0);
+    if (lane == 31) { wsum[wid] = x; wits[wid] = y; }
+    if (lane == 0) wact[wid] = __popc(act);
+    __syncthreads();
+    long long xb = 0, yb = 0;
+    int ab = 0;
+    for (int k = 0; k < wid; k++) { xb += wsum[k]; yb += wits[k]; ab += wact[k]; }
+    const long long carry = carry_s, icarry = icarry_s;
+    const int acar = act_s;
+    if (i < P.ng) {
+      P.cell_off[i] = (int)(carry + xb + x - v);
+      if (v > 0) {
+        const int ai = acar + ab + __popc(act & ((1u << lane) - 1u));
+        P.act_cells[ai] = i;
+        P.item_off[ai] = icarry + yb + y - it;
+      }
+    }
+    __syncthreads();
+    if (t == 0) {
+      long long xs = 0, ys = 0;
+      int as = 0;
+      for (int k = 0; k < 32; k++) { xs += wsum[k]; ys += wits[k]; as += wact[k]; }
+      carry_s = carry + xs;
+      icarry_s = icarry + ys;
+      act_s = acar + as;
+    }
+    __syncthreads();
+  }
+  if (t == 0) {
+    P.cell_off[P.ng] = (int)carry_s;
+    P.item_off[act_s] = icarry_s;
+    *P.n_act = act_s;
+    P.ctr[5] = (unsigned long long)carry_s;
+  }
+}
+
+__global__ void k_cell_fill(TraceDev P, const unsigned *bits) {
+  const int lane = threadIdx.x & 31;
+  const int nwarp = (gridDim.x * blockDim.x) >> 5;
+  for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < P.ng; cell += nwarp) {
+    const unsigned *row = bits + (size_t)cell * P.W;
+    long long pos = P.cell_off[cell];
+    if (pos == P.cell_off[cell + 1]) continue;
+    for (int w0 = 0; w0 < P.W; w0 += 32) {
+      const int w = w0 + lane;
+      unsigned b = w < P.W ? row[w] : 0u;
+      const int c = __popc(b);
+      int x = c;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      long long q = pos + x - c;
+      while (b) {
+        const int k = __ffs(b) - 1;
+        b &= b - 1u;
+        if ((unsigned long long)q < P.task_cap) P.task_slot[q] = w * 32 + k;
+        else atomicOr(P.err, AMS_DERR_TASKS);
+        q++;
+      }
+      pos += __shfl_sync(0xffffffffu, x, 31);
     }
   }
 }
 
 // ---------------------------------------------------------------- stage 2
-// 5 CTAs of 256 per SM (48 registers, some spills): 2.51 ms per coverage-128
-// trace and 2.20 s per ms-256 channel set, against 2.66 / 2.26 at 4 CTAs
-// (64 registers), 2.51 / 2.26 at 6 and 2.84 / 2.86 at 8
-__global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P, unsigned long long n_tasks) {
-  const int S = P.n_src;
-  const int per_cell = P.gs * P.gs;
-  const unsigned long long per_task = (unsigned long long)per_cell * S;
-  const unsigned long long n_rays = n_tasks * per_task;
-  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31;
+// One backward ray (stage-2 raygen + closest-hit programs,
+// optixPathTracer.cu:191-273, :332-417): the image source of the path key in
+// `slot` seen from Rx position o, traced back to Tx `s`.  Returns true with
+// the contribution as 2^-56 fixed point when the ray arrives.
+__device__ __forceinline__ bool s2_ray(const TraceDev &P, int slot, int s, af3 o, af3 srcdir,
+                                       af3 dstdir, unsigned &segs, unsigned long long &cre,
+                                       unsigned long long &cim) {
+  const int32_t *key = P.tab_key + (size_t)slot * 14;
+  Mat34 M;
+#pragma unroll
+  for (int k = 0; k < 12; k++) M.m[k] = __int_as_float(key_word(key, k));
+  const int hc = key_word(key, 12), mask = key_word(key, 13);
   const float lam = P.lam_f;
+  af3 d = nrm3(sub3(image_of(M, ld3(P.src + 3 * s)), o));
+  float amp = beampattern(d, dstdir, P.dst_bp);
+  float far = 1e6f, dd = 0.0f, dres = 0.0f;
+  double D = 0.0;
+  int ttl = hc + 1;
+  int guard = 0;
+  bool ok = false;
+  while (ttl > 0) {
+    if (++guard > AMS_SEG_CAP) { atomicOr(P.err, AMS_DERR_LOOP); break; }
+    Hit h = closest(P, o, d, 3);
+    segs++;
+    if (h.inst == 3) break;
+    const float t = h.t;
+    o = add3(o, scl3(d, t));
+    dd += t;
+    D += (double)t;
+    if (h.inst == 0) {
+      if (ttl == 1) break;
+      af3 v0, v1, v2;
+      scene_tri(P, h.prim, v0, v1, v2);
+      af3 N0 = nrm3(cross3(sub3(v1, v0), sub3(v2, v0)));
+      af3 N = faceforward3(N0, neg3(d), N0);
+      int m = __ldg(P.mat + h.prim);
+      float ct = dot3(d, N) / (len3(N) * len3(d));
+      float loss = fabsf(__ldg(P.mat_prop + theta_id(ct) + m * AMS_NBINS));
+      ttl--;
+      int hcb = hc + 1 - ttl;
+      int is_ref = (mask >> (hcb - 1)) & 1;
+      float max_d = fmaxf(fmaxf(len3(sub3(v0, v1)), len3(sub3(v1, v2))), len3(sub3(v2, v0)));
+      float fspl = 1.0f;
+      if (dd > far) { fspl = lam / ((4.0f * AMS_PIF) * dres); dres = 0.0f; }
+      amp *= loss * fspl;
+      dres += dd;
+      // far_dist = 2 max_d^2 / lambda, divided in double and rounded to
+      // float (optixPathTracer.cu:385-389).  Its value matters only when
+      // the segment is longer; a float estimate (relative error < 3e-7)
+      // with a 1e-5 margin settles the common near-field case without
+      // the double division (FP64 is slow on this part).
+      float far_next = 1e6f;
+      if (dd > ((2.0f * max_d) * max_d / lam) * 0.99999f) {
+        const float fd = (float)(2.0 * (double)max_d * (double)max_d / (double)lam);
+        far_next = (dd > fd) ? fd : 1e6f;
+      }
+      far = far_next;
+      dd = 0.0f;
+      if (is_ref) d = sub3(d, scl3(N, 2.0f * dot3(d, N)));
+    } else if (h.inst == 1 && h.prim == s) {
+      if (ttl == 1) {
+        float bp = beampattern(neg3(d), srcdir, P.src_bp);
+        float af = lam / ((4.0f * AMS_PIF) * (dres + dd));
+        amp *= bp * af;
+        ok = true;
+      }
+      break;
+    }
+  }
+  if (ok) {
+    // FP64 path length -> phase, reduced mod 2 pi in FP64 (products with
+    // precomputed 2 pi / lambda and 1 / (2 pi): no FP64 division per ray)
+    double ph = D * P.two_pi_over_lam;
+    ph = ph - 6.283185307179586 * floor(ph * 0.15915494309189535);
+    float sn, cs;
+    sincosf((float)ph, &sn, &cs);
+    double re = (double)(amp * cs), im = (double)(-amp * sn);
+    if (!(fabs(re) < AMS_ACC_LIMIT && fabs(im) < AMS_ACC_LIMIT)) {
+      atomicOr(P.err, AMS_DERR_ACC_RANGE);
+      return false;
+    }
+    cre = (unsigned long long)__double2ll_rn(re * AMS_ACC_SCALE);
+    cim = (unsigned long long)__double2ll_rn(im * AMS_ACC_SCALE);
+  }
+  return ok;
+}
+
+// Persistent stage 2: a warp takes an item = (active cell, a chunk of up to
+// kpi of the cell's new paths, 32 consecutive (Rx within the cell, Tx)
+// pairs, Tx fastest) and traces the chunk's paths one after the other; each
+// lane sums its pair's contributions over the chunk in registers (exact
+// 64-bit fixed point) and adds them once into the Rx-major accumulator
+// acc[dst][s], so a warp's adds cover one or a few contiguous runs of Tx
+// (coalesced), one atomic add per (Tx, Rx) and chunk instead of two per
+// verified ray.  The lanes of an item trace the same path key from the same
+// Rx to neighbouring Tx elements: nearly identical rays.  Items are fetched
+// dynamically (one counter per warp); kpi is chosen per round by the host so
+// that a round still has several items per resident warp.
+__global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
+  const int S = P.n_src;
+  const long long pairs = (long long)P.gs * P.gs * S;
+  const long long G = (pairs + 31) / 32;
+  const int n_act = *P.n_act;
+  const long long n_items = P.item_off[n_act];
+  const int lane = threadIdx.x & 31;
   const af3 srcdir = mk3(P.src_dir[0], P.src_dir[1], P.src_dir[2]);
   const af3 dstdir = mk3(P.dst_dir[0], P.dst_dir[1], P.dst_dir[2]);
-  for (unsigned long long base = (unsigned long long)blockIdx.x * blockDim.x; base < n_rays;
-       base += stride) {
-    const unsigned long long ray = base + threadIdx.x;
-    bool valid = ray < n_rays;
-    long long task = -1;
-    bool ok = false, traced = false;
+  unsigned long long n_ok = 0, n_fail = 0, n_segs = 0;
+  while (true) {
+    unsigned long long item = 0;
+    if (lane == 0) item = atomicAdd(P.ctr + 11, 1ull);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if ((long long)item >= n_items) break;
+    // the active cell whose item range holds `item` (binary search)
+    int lo = 0, hi = n_act - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(P.item_off + mid) <= (long long)item) lo = mid; else hi = mid - 1;
+    }
+    const long long local = (long long)item - __ldg(P.item_off + lo);
+    const int cell = __ldg(P.act_cells + lo);
+    const int c0 = __ldg(P.cell_off + cell), c1 = __ldg(P.cell_off + cell + 1);
+    if (c0 < 0 || c1 < c0 || (unsigned long long)c1 > P.task_cap) {
+      if (lane == 0) atomicOr(P.err, AMS_DERR_TASKS);
+      continue;
+    }
+    const int t0 = c0 + (int)(local / G) * P.kpi, t1 = min(c1, t0 + P.kpi);
+    const long long pr = (local % G) * 32 + lane;
+    bool act = pr < pairs;
+    const int inner = act ? (int)(pr / S) : 0, s = act ? (int)(pr % S) : 0;
+    const int gi = cell / P.n1g, gj = cell % P.n1g;
+    const int di = inner / P.gs + gi * P.gs, dj = inner % P.gs + gj * P.gs;
+    const int dst = di * P.n1_dst + dj;
+    if (dst >= P.n_dst || (P.strict_grid && (di >= P.n0_dst || dj >= P.n1_dst))) act = false;
+    const af3 o = act ? ld3(P.dst + 3 * dst) : mk3(0.f, 0.f, 0.f);
+    unsigned long long sre = 0, sim = 0;
     unsigned segs = 0;
-    int cell = 0, slot = 0, inner = 0, s = 0;
-    if (valid) {
-      task = (long long)(ray / per_task);
-      unsigned long long rem = ray % per_task;
-      inner = (int)(rem / S);
-      s = (int)(rem % S);
-      const int2 tk = P.tasks[task];
-      cell = tk.x;
-      slot = tk.y;
-      if ((unsigned)cell >= (unsigned)P.ng || (unsigned)slot > P.tab_mask) {
-        atomicOr(P.err, AMS_DERR_TASKS);
-        cell = 0;
-        slot = 0;
-        valid = false;
+    for (int t = t0; t < t1; t++) {
+      const int slot = __ldg(P.task_slot + t);
+      if ((unsigned)slot > P.tab_mask) {
+        if (lane == 0) atomicOr(P.err, AMS_DERR_TASKS);
+        break;
       }
-    }
-    if (valid) {
-      const int gi = cell / P.n1g, gj = cell % P.n1g;
-      const int di = inner / P.gs + gi * P.gs, dj = inner % P.gs + gj * P.gs;
-      const int dst = di * P.n1_dst + dj;
-      bool skip = dst >= P.n_dst || (P.strict_grid && (di >= P.n0_dst || dj >= P.n1_dst));
-      if (!skip) {
-        traced = true;
-        const int32_t *key = P.tab_key + (size_t)slot * 14;
-        Mat34 M;
-#pragma unroll
-        for (int k = 0; k < 12; k++) M.m[k] = __int_as_float(__ldg(key + k));
-        const int hc = __ldg(key + 12), mask = __ldg(key + 13);
-        af3 o = ld3(P.dst + 3 * dst);
-        af3 d = nrm3(sub3(image_of(M, ld3(P.src + 3 * s)), o));
-        float amp = beampattern(d, dstdir, P.dst_bp);
-        float far = 1e6f, dd = 0.0f, dres = 0.0f;
-        double D = 0.0;
-        int ttl = hc + 1;
-        int guard = 0;
-        while (ttl > 0) {
-          if (++guard > AMS_SEG_CAP) { atomicOr(P.err, AMS_DERR_LOOP); break; }
-          Hit h = closest(P, o, d, 3);
-          segs++;
-          if (h.inst == 3) break;
-          const float t = h.t;
-          o = add3(o, scl3(d, t));
-          dd += t;
-          D += (double)t;
-          if (h.inst == 0) {
-            if (ttl == 1) break;
-            af3 v0, v1, v2;
-            scene_tri(P, h.prim, v0, v1, v2);
-            af3 N0 = nrm3(cross3(sub3(v1, v0), sub3(v2, v0)));
-            af3 N = faceforward3(N0, neg3(d), N0);
-            int m = __ldg(P.mat + h.prim);
-            float ct = dot3(d, N) / (len3(N) * len3(d));
-            float loss = fabsf(__ldg(P.mat_prop + theta_id(ct) + m * AMS_NBINS));
-            ttl--;
-            int hcb = hc + 1 - ttl;
-            int is_ref = (mask >> (hcb - 1)) & 1;
-            float max_d = fmaxf(fmaxf(len3(sub3(v0, v1)), len3(sub3(v1, v2))), len3(sub3(v2, v0)));
-            float fspl = 1.0f;
-            if (dd > far) { fspl = lam / ((4.0f * AMS_PIF) * dres); dres = 0.0f; }
-            amp *= loss * fspl;
-            dres += dd;
-            // far_dist = 2 max_d^2 / lambda, divided in double and rounded to
-            // float (optixPathTracer.cu:385-389).  Its value matters only when
-            // the segment is longer; a float estimate (relative error < 3e-7)
-            // with a 1e-5 margin settles the common near-field case without
-            // the double division (FP64 is slow on this part).
-            float far_next = 1e6f;
-            if (dd > ((2.0f * max_d) * max_d / lam) * 0.99999f) {
-              const float fd = (float)(2.0 * (double)max_d * (double)max_d / (double)lam);
-              far_next = (dd > fd) ? fd : 1e6f;
-            }
-            far = far_next;
-            dd = 0.0f;
-            if (is_ref) d = sub3(d, scl3(N, 2.0f * dot3(d, N)));
-          } else if (h.inst == 1 && h.prim == s) {
-            if (ttl == 1) {
-              float bp = beampattern(neg3(d), srcdir, P.src_bp);
-              float af = lam / ((4.0f * AMS_PIF) * (dres + dd));
-              amp *= bp * af;
-              ok = true;
-            }
-            break;
-          }
-        }
-        if (ok) {
-          // FP64 path length -> phase, reduced mod 2 pi in FP64 (products with
-          // precomputed 2 pi / lambda and 1 / (2 pi): no FP64 division per ray)
-          double ph = D * P.two_pi_over_lam;
-          ph = ph - 6.283185307179586 * floor(ph * 0.15915494309189535);
-          float sn, cs;
-          sincosf((float)ph, &sn, &cs);
-          double re = (double)(amp * cs), im = (double)(-amp * sn);
-          if (!(fabs(re) < AMS_ACC_LIMIT && fabs(im) < AMS_ACC_LIMIT)) {
-            atomicOr(P.err, AMS_DERR_ACC_RANGE);
-          } else {
-            unsigned long long *a = P.acc + ((size_t)s * P.n_dst + dst) * 2;
-            atomicAdd(a, (unsigned long long)__double2ll_rn(re * AMS_ACC_SCALE));
-            atomicAdd(a + 1, (unsigned long long)__double2ll_rn(im * AMS_ACC_SCALE));
-          }
-        }
+      bool ok = false;
+      if (act) {
+        unsigned long long cre = 0, cim = 0;
+        ok = s2_ray(P, slot, s, o, srcdir, dstdir, segs, cre, cim);
+        if (ok) { sre += cre; sim += cim; n_ok++; } else { n_fail++; }
       }
+      if (__any_sync(0xffffffffu, ok) && lane == 0)
+        atomicOr(P.S + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
     }
-    // counters and the success bit of each task, one atomic per warp / task
-    unsigned okb = __ballot_sync(0xffffffffu, ok);
-    unsigned trb = __ballot_sync(0xffffffffu, traced);
-    for (int off = 16; off > 0; off >>= 1) segs += __shfl_xor_sync(0xffffffffu, segs, off);
-    if (lane == 0) {
-      if (segs) atomicAdd(P.ctr + 9, (unsigned long long)segs);
-      if (okb) atomicAdd(P.ctr + 3, (unsigned long long)__popc(okb));
-      if (trb & ~okb) atomicAdd(P.ctr + 4, (unsigned long long)__popc(trb & ~okb));
+    n_segs += segs;
+    if (act && (sre | sim)) {
+      unsigned long long *acc = P.acc + ((size_t)dst * S + s) * 2;
+      atomicAdd(acc, sre);
+      atomicAdd(acc + 1, sim);
     }
-    unsigned same = __match_any_sync(0xffffffffu, task);
-    unsigned any_ok = okb & same;
-    if (valid && any_ok && lane == __ffs(same) - 1)
-      atomicOr(P.S + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    n_ok += __shfl_xor_sync(0xffffffffu, n_ok, off);
+    n_fail += __shfl_xor_sync(0xffffffffu, n_fail, off);
+    n_segs += __shfl_xor_sync(0xffffffffu, n_segs, off);
+  }
+  if (lane == 0) {
+    if (n_segs) atomicAdd(P.ctr + 9, n_segs);
+    if (n_ok) atomicAdd(P.ctr + 3, n_ok);
+    if (n_fail) atomicAdd(P.ctr + 4, n_fail);
   }
 }
 
@@ -987,11 +1147,34 @@ __global__ void k_popcount(const unsigned *bits, long long n, unsigned long long
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
-__global__ void k_finalize(const unsigned long long *acc, float *result, long long n) {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    long long v = (long long)acc[i];
-    if (v) result[i] += (float)((double)v * AMS_ACC_INV);
+// result[s][dst] += acc[dst][s] * 2^-56 (re, im): 32 x 32 tiles turned
+// through shared memory, reads coalesced over s and writes over dst.
+// Block (32, 8), grid (ceil(n_dst / 32), ceil(n_src / 32)).
+__global__ void k_finalize(const unsigned long long *acc, float *result, int n_src, int n_dst) {
+  __shared__ float2 tl[32][33];
+  const int d0 = blockIdx.x * 32, s0 = blockIdx.y * 32;
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int d = d0 + i, s = s0 + threadIdx.x;
+    float2 v = make_float2(0.f, 0.f);
+    if (d < n_dst && s < n_src) {
+      const unsigned long long *a = acc + ((size_t)d * n_src + s) * 2;
+      v = make_float2((float)((double)(long long)a[0] * AMS_ACC_INV),
+                      (float)((double)(long long)a[1] * AMS_ACC_INV));
+    }
+    tl[i][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+    const int s = s0 + i, d = d0 + threadIdx.x;
+    if (s >= n_src || d >= n_dst) continue;
+    const float2 v = tl[threadIdx.x][i];
+    if (v.x != 0.f || v.y != 0.f) {
+      float2 *r = reinterpret_cast<float2 *>(result) + (size_t)s * n_dst + d;
+      float2 x = *r;
+      x.x += v.x;
+      x.y += v.y;
+      *r = x;
+    }
   }
 }
 
@@ -1000,7 +1183,8 @@ __global__ void k_export(TraceDev P, int32_t *out, unsigned long long *n_out) {
        s += gridDim.x * blockDim.x) {
     if (P.tab_h[s] == 0ull) continue;
     unsigned long long k = atomicAdd(n_out, 1ull);
-    for (int i = 0; i < 14; i++) out[k * 14 + i] = P.tab_key[(size_t)s * 14 + i];
+    for (int i = 0; i < 14; i++)
+      out[k * 14 + i] = (int32_t)((uint32_t)P.tab_key[(size_t)s * 14 + i] ^ AMS_KEY_FLIP);
   }
 }
 
@@ -1018,36 +1202,70 @@ cudaError_t trace_stage1(const TraceDev &P, cudaStream_t st) {
   // persistent: as many CTAs as are resident at once (lanes fetch launch
   // indices from ctr[10], zeroed with the other counters)
   long long n = (long long)P.launch_x * P.launch_y;
-  static int per_sm[AMS_MAX_DEVICES] = {0};
+  // the smallest slot array that holds max_reflection's slots
+  const int lk = P.L <= 2 ? 0 : (P.L == 3 ? 1 : 2);
+  void (*const kern[3])(TraceDev) = {k_stage1<2>, k_stage1<3>, k_stage1<AMS_MAX_L>};
+  static int per_sm[3][AMS_MAX_DEVICES] = {{0}};
   const int dev = ams_current_device();
   if (dev < 0) return cudaErrorInvalidDevice;
-  if (per_sm[dev] == 0) {
+  if (per_sm[lk][dev] == 0) {
     int b = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_stage1, 128, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern[lk], 128, 0);
     if (e != cudaSuccess) return e;
-    per_sm[dev] = b > 0 ? b : 1;
+    per_sm[lk][dev] = b > 0 ? b : 1;
   }
-  long long blocks = (long long)per_sm[dev] * ams_device_sms();
+  long long blocks = (long long)per_sm[lk][dev] * ams_device_sms();
   const long long need = (n + 127) / 128;
   if (blocks > need) blocks = need;
   if (blocks < 1) blocks = 1;
-  k_stage1<<<(int)blocks, 128, 0, st>>>(P);
+  kern[lk]<<<(int)blocks, 128, 0, st>>>(P);
   return cudaGetLastError();
 }
 
+namespace {
+int stage2_per_sm() {
+  static int per_sm[AMS_MAX_DEVICES] = {0};
+  const int dev = ams_current_device();
+  if (dev < 0) return 1;
+  if (per_sm[dev] == 0) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_stage2, 256, 0) != cudaSuccess) b = 1;
+    per_sm[dev] = b > 0 ? b : 1;
+  }
+  return per_sm[dev];
+}
+}  // namespace
+
+int trace_paths_per_item(const TraceDev &P, unsigned long long n_tasks) {
+  // about 4 items per resident warp when every item takes one path; larger
+  // chunks (fewer atomic adds, longer items) only when the round is big
+  const unsigned long long warps = (unsigned long long)stage2_per_sm() * ams_device_sms() * 8;
+  const unsigned long long pairs = (unsigned long long)(P.gs * P.gs) * P.n_src;
+  const unsigned long long work = n_tasks * ((pairs + 31) / 32);
+  unsigned long long k = work / (4 * warps);
+  if (k < 1) k = 1;
+  if (k > 16) k = 16;
+  return (int)k;
+}
+
 cudaError_t trace_make_tasks(const TraceDev &P, const unsigned *bits, cudaStream_t st) {
-  long long n = (long long)P.ng * P.W;
-  k_make_tasks<<<grid_for(n, 256), 256, 0, st>>>(P, bits);
+  const long long threads = (long long)P.ng * 32;
+  k_cell_counts<<<grid_for(threads, 256), 256, 0, st>>>(P, bits);
+  k_cell_scan<<<1, 1024, 0, st>>>(P);
+  k_cell_fill<<<grid_for(threads, 256), 256, 0, st>>>(P, bits);
   return cudaGetLastError();
 }
 
 cudaError_t trace_stage2(const TraceDev &P, unsigned long long n_tasks, cudaStream_t st) {
   if (n_tasks == 0) return cudaSuccess;
-  unsigned long long rays = n_tasks * (unsigned long long)(P.gs * P.gs) * P.n_src;
-  long long blocks = (long long)((rays + 255) / 256);
-  const long long cap = (long long)ams_device_sms() * 8 * 16;
-  if (blocks > cap) blocks = cap;
-  k_stage2<<<(int)blocks, 256, 0, st>>>(P, n_tasks);
+  // persistent: as many CTAs as are resident, fewer for a small round
+  const unsigned long long pairs = (unsigned long long)(P.gs * P.gs) * P.n_src;
+  const unsigned long long items_max = n_tasks * ((pairs + 31) / 32);
+  long long blocks = (long long)stage2_per_sm() * ams_device_sms();
+  const long long need = (long long)((items_max + 7) / 8);
+  if (blocks > need) blocks = need;
+  if (blocks < 1) blocks = 1;
+  k_stage2<<<(int)blocks, 256, 0, st>>>(P);
   return cudaGetLastError();
 }
 
@@ -1066,8 +1284,8 @@ cudaError_t trace_count_bits(const TraceDev &P, const unsigned *bits, unsigned l
 }
 
 cudaError_t trace_finalize(const TraceDev &P, float *result, cudaStream_t st) {
-  long long n = (long long)P.n_src * P.n_dst * 2;
-  k_finalize<<<grid_for(n, 256), 256, 0, st>>>(P.acc, result, n);
+  dim3 grid((P.n_dst + 31) / 32, (P.n_src + 31) / 32), block(32, 8);
+  k_finalize<<<grid, block, 0, st>>>(P.acc, result, P.n_src, P.n_dst);
   return cudaGetLastError();
 }
 

@@ -7,7 +7,7 @@
 
 // device error flags (bits of TraceDev::err)
 #define AMS_DERR_PATH_TABLE 1u    // path table full
-#define AMS_DERR_HASH 2u          // 64-bit hash collision between distinct keys
+#define AMS_DERR_HASH 2u          // a path-table slot's key words never appeared
 #define AMS_DERR_STACK 4u         // traversal stack overflow
 #define AMS_DERR_ACC_RANGE 8u     // contribution outside the fixed-point range
 #define AMS_DERR_TASKS 16u        // task list overflow
@@ -45,8 +45,7 @@ struct TraceDev {
   int src_bp, dst_bp;
   // path table (open addressing, slot = path id)
   unsigned long long *tab_h;
-  unsigned *tab_chk;
-  int32_t *tab_key;  // 14 words per slot
+  int32_t *tab_key;  // 14 words per slot, sign bits flipped (0 = not written yet)
   unsigned tab_mask;
   unsigned tab_limit;  // occupied slots above this -> grow and retry
   // task bitmaps [ng][W] in slot space
@@ -54,19 +53,30 @@ struct TraceDev {
   unsigned *N;  // new this round
   unsigned *S;  // succeeded this round
   int W;
-  // task list of the current round
-  int2 *tasks;
+  // tasks of the current round per cell: slots task_slot[cell_off[c] ..
+  // cell_off[c + 1]) of cell c; cells with tasks act_cells[0 .. *n_act),
+  // active cell a owning stage-2 items item_off[a] .. item_off[a + 1)
+  int *task_slot;
   unsigned long long task_cap;
-  // fixed-point channel accumulators [n_src * n_dst * 2]
+  int *cell_off;        // [ng + 1]
+  int *act_cells;       // [ng]
+  long long *item_off;  // [ng + 1]
+  int *n_act;
+  int kpi;              // paths per stage-2 item this round
+  // fixed-point channel accumulators, Rx-major: acc[(dst * n_src + s) * 2]
   unsigned long long *acc;
   // counters: 0 records, 1 overflow threads, 2 occupied slots, 3 ok rays,
   // 4 failed rays, 5 tasks this round, 6 unique records, 7 new tasks,
-  // 8 stage-1 closest-hit queries, 9 stage-2 closest-hit queries
+  // 8 stage-1 closest-hit queries, 9 stage-2 closest-hit queries,
+  // 10 stage-1 launch-index fetch, 11 stage-2 item fetch
   unsigned long long *ctr;
   unsigned *err;
 };
 
 cudaError_t trace_stage1(const TraceDev &P, cudaStream_t st);
+// paths per stage-2 item for a round of n_tasks tasks (set P.kpi before
+// listing the round's tasks)
+int trace_paths_per_item(const TraceDev &P, unsigned long long n_tasks);
 cudaError_t trace_make_tasks(const TraceDev &P, const unsigned *bits, cudaStream_t st);
 cudaError_t trace_stage2(const TraceDev &P, unsigned long long n_tasks, cudaStream_t st);
 cudaError_t trace_expand(const TraceDev &P, cudaStream_t st);
