@@ -253,7 +253,7 @@ def screening_report(study, mlp, pool_params, pool_gain, top_frac=0.05, t_trial=
     }
 
 
-def batch_evaluate(cfg, indices=None, workers=4, opt_steps=20, lr=0.3):
+def batch_evaluate(cfg, indices=None, workers=4, opt_steps=20, lr=0.3, keep=False):
     """Batched hyper-configs (scenes.batch_config): for each placement the
     AP->Rx channel with the metasurface as a blackhole, the AP->MS and MS->Rx
     channels (build_channels, go.py:1135-1247), then opt_steps Adam steps of
@@ -262,7 +262,12 @@ def batch_evaluate(cfg, indices=None, workers=4, opt_steps=20, lr=0.3):
 
     Placements run on `workers` host threads, each with its own CUDA stream
     and scene handle, so one placement's flood-fill round trips overlap the
-    others' kernels.  Returns per-placement results and the wall time."""
+    others' kernels.  Returns per-placement results and the wall time.  Each
+    result has the loss of the first and the last step, and ms_share: the
+    power the metasurface path carries at phi = 0 over the power of the
+    direct channel, summed over the Rx grid (after the timed work).  With
+    keep=True a result also holds the channels, the weights and the final
+    phase map (keys H, w, phi)."""
     import concurrent.futures as cf
     import threading
 
@@ -314,12 +319,22 @@ def batch_evaluate(cfg, indices=None, workers=4, opt_steps=20, lr=0.3):
                 first = lv if first is None else first
                 last = lv
             first_v, last_v = float(first), float(last)
+            obj.check_status(plan)
             plan.close()
             local.stream.synchronize()
             t2 = time.perf_counter()
-        return dict(index=pi, size=pl["size"], M=M, rx_paths=sd["rx_paths"] + sa["rx_paths"] + sr["rx_paths"],
-                    ms_to_rx_paths=sr["rx_paths"], t_trace=t1 - t0, t_opt=t2 - t1,
-                    loss_first=first_v, loss_last=last_v)
+            with torch.no_grad():
+                yd = (w @ Hd).abs().pow(2).sum()
+                ym = ((w @ Ha) @ Hr).abs().pow(2).sum()
+                share = float(ym / yd) if float(yd) > 0 else float("inf")
+        out = dict(index=pi, size=pl["size"], M=M,
+                   rx_paths=sd["rx_paths"] + sa["rx_paths"] + sr["rx_paths"],
+                   ms_to_rx_paths=sr["rx_paths"], ap_to_ms_paths=sa["rx_paths"],
+                   t_trace=t1 - t0, t_opt=t2 - t1, loss_first=first_v, loss_last=last_v,
+                   ms_share=share)
+        if keep:
+            out.update(H=(Hd, Ha, Hr), w=w, phi=phi.detach().clone())
+        return out
 
     torch.cuda.synchronize()
     t0 = time.perf_counter()

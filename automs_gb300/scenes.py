@@ -306,8 +306,10 @@ def batch_config(n_place=64, seed=0, target_tris=200_000, n_rx=256, launch=1000)
     """Batched hyper-configs: a multi-room building (multiroom_scene), a
     16-element AP in the middle room at 2.5 m facing +y, an n_rx x n_rx Rx
     grid over the footprint at 1.5 m, and n_place metasurfaces of n x n
-    elements (n uniform over 16, 24, ..., 64) at lambda/2 on seeded outer-wall
-    positions facing into the building, 1 mm off the wall."""
+    elements (n uniform over 16, 24, ..., 64) at lambda/2 on seeded positions
+    of the four walls of the AP's room, facing into the room 1 mm off the
+    wall (where the AP illuminates them, as the reference's trial places its
+    metasurface on a wall the AP sees, physical_exp_nni_model.py:29-73)."""
     rng = np.random.Generator(np.random.PCG64(1000 + seed))
     tris, mat, mat_prop, xs, ys = multiroom_scene(target_tris, seed=seed)
     X, Y = xs[-1], ys[-1]
@@ -316,10 +318,11 @@ def batch_config(n_place=64, seed=0, target_tris=200_000, n_rx=256, launch=1000)
     ap = ((xs[ci] + xs[ci + 1]) / 2, (ys[cj] + ys[cj + 1]) / 2, 2.5)
     src = ula(ap, (1, 0, 0), 16, lam / 2)
     dst = rx_grid(0.25, X - 0.25, n_rx, 0.25, Y - 0.25, n_rx, 1.5)
-    walls = [((0.0, 0.0), (1.0, 0.0), (0.0, 1.0), X),       # y = 0, normal +y
-             ((0.0, Y), (1.0, 0.0), (0.0, -1.0), X),         # y = Y, normal -y
-             ((0.0, 0.0), (0.0, 1.0), (1.0, 0.0), Y),        # x = 0, normal +x
-             ((X, 0.0), (0.0, 1.0), (-1.0, 0.0), Y)]         # x = X, normal -x
+    x0, x1, y0, y1 = xs[ci], xs[ci + 1], ys[cj], ys[cj + 1]
+    walls = [((x0, y0), (1.0, 0.0), (0.0, 1.0), x1 - x0),    # y = y0, normal +y
+             ((x0, y1), (1.0, 0.0), (0.0, -1.0), x1 - x0),   # y = y1, normal -y
+             ((x0, y0), (0.0, 1.0), (1.0, 0.0), y1 - y0),    # x = x0, normal +x
+             ((x1, y0), (0.0, 1.0), (-1.0, 0.0), y1 - y0)]   # x = x1, normal -x
     place = []
     for _ in range(n_place):
         w = int(rng.integers(0, 4))

@@ -173,10 +173,12 @@ def launch_pathtrace(result, src, dst, src_aabb_buffer, dst_aabb_buffer, scene_t
 def build_channel(src, dst, src_dir, dst_dir, src_bptype, dst_bptype, wave_len, scene_folder,
                   max_reflection=4, dst_radius=0.06, src_radius=0.5e-5, samples_per_launch=1,
                   reserved_size=100, blackhole_buffer=[], reflector_buffer=[], door_buffer=[],
-                  dst_gridsize=5, launch=(100, 100), scene=None, return_stats=False):
+                  dst_gridsize=5, launch=(100, 100), scene=None, return_stats=False,
+                  return_paths=False):
     """build_channel of go.py:623-767.  Extra keywords: `launch` (the
     reference hard-codes 100 x 100, go.py:739-740), `scene` (a prebuilt
-    Scene instead of the folder), `return_stats`."""
+    Scene instead of the folder), `return_stats` (also return the trace's
+    counters), `return_paths` (also return its ordered path list)."""
     own = scene is None
     if own:
         scene = Scene.from_folder(scene_folder, blackhole_buffer, reflector_buffer, door_buffer)
@@ -187,42 +189,58 @@ def build_channel(src, dst, src_dir, dst_dir, src_bptype, dst_bptype, wave_len, 
                     samples_per_launch)
     src_buffer = torch.cat([src - src_radius, src + src_radius], dim=-1)
     dst_buffer = torch.cat([dst - dst_radius, dst + dst_radius], dim=-1)
+    paths = None
     try:
         res, st = scene.trace(src, dst, p, src_aabb=src_buffer, dst_aabb=dst_buffer)
+        if return_paths:
+            paths = scene.export_paths()
     finally:
         if own:
             scene.close()
     H = torch.complex(res[..., 0], res[..., 1])
-    return (H, st) if return_stats else H
+    out = (H,) + ((st,) if return_stats else ()) + ((paths,) if return_paths else ())
+    return out if len(out) > 1 else H
 
 
 def build_channels(src, dst, ms_list, ap_dir, scene_folder, wave_len, max_reflection,
-                   reflector_buffer=[], door_buffer=[], launch=(100, 100)):
+                   reflector_buffer=[], door_buffer=[], launch=(100, 100), details=None):
     """build_channels of go.py:1135-1247: keys src_to_dst, src_to_ms{i},
-    ms{i}_to_dst, ms{i}_to_ms{j}; AP beam type 2, MS 1, Rx 0; the other
-    metasurfaces are blackholes in each trace."""
+    ms{i}_to_dst, ms{i}_to_ms{j} in the reference's order; AP beam type 2,
+    MS 1, Rx 0; the other metasurfaces are blackholes in each trace.  With a
+    dict as `details`, details[key] = (counters, ordered path list) of each
+    trace."""
     dir_no = torch.tensor([0, 0, 0], dtype=torch.float32)
     if isinstance(ap_dir, list):
         ap_dir = torch.tensor(ap_dir, dtype=torch.float32)
     n = len(ms_list)
     ch = {}
-    kw = dict(reflector_buffer=reflector_buffer, door_buffer=door_buffer, launch=launch)
-    ch["src_to_dst"] = build_channel(src, dst, ap_dir, dir_no, 2, 0, wave_len, scene_folder,
-                                     max_reflection,
-                                     blackhole_buffer=[ms_list[i].blackhole for i in range(n)], **kw)
+    want = details is not None
+    kw = dict(reflector_buffer=reflector_buffer, door_buffer=door_buffer, launch=launch,
+              return_stats=want, return_paths=want)
+
+    def put(key, out):
+        if want:
+            ch[key], st, paths = out
+            details[key] = (st, paths)
+        else:
+            ch[key] = out
+    put("src_to_dst", build_channel(src, dst, ap_dir, dir_no, 2, 0, wave_len, scene_folder,
+                                    max_reflection,
+                                    blackhole_buffer=[ms_list[i].blackhole for i in range(n)],
+                                    **kw))
     for i in range(n):
         others = [ms_list[k].blackhole for k in range(n) if k != i]
-        ch["src_to_ms{%d}" % i] = build_channel(src, ms_list[i].pos, ap_dir, ms_list[i].recv_dir,
-                                                2, 1, wave_len, scene_folder, max_reflection,
-                                                blackhole_buffer=others, **kw)
-        ch["ms{%d}_to_dst" % i] = build_channel(ms_list[i].pos, dst, ms_list[i].send_dir, dir_no,
-                                                1, 0, wave_len, scene_folder, max_reflection,
-                                                blackhole_buffer=others, **kw)
+        put("src_to_ms{%d}" % i, build_channel(src, ms_list[i].pos, ap_dir, ms_list[i].recv_dir,
+                                               2, 1, wave_len, scene_folder, max_reflection,
+                                               blackhole_buffer=others, **kw))
+        put("ms{%d}_to_dst" % i, build_channel(ms_list[i].pos, dst, ms_list[i].send_dir, dir_no,
+                                               1, 0, wave_len, scene_folder, max_reflection,
+                                               blackhole_buffer=others, **kw))
         for j in range(i + 1, n):
             bh = [ms_list[k].blackhole for k in range(n) if k != i and k != j]
-            ch["ms{%d}_to_ms{%d}" % (i, j)] = build_channel(
+            put("ms{%d}_to_ms{%d}" % (i, j), build_channel(
                 ms_list[i].pos, ms_list[j].pos, ms_list[i].send_dir, ms_list[j].recv_dir, 1, 1,
-                wave_len, scene_folder, max_reflection, blackhole_buffer=bh, **kw)
+                wave_len, scene_folder, max_reflection, blackhole_buffer=bh, **kw))
     return ch
 
 

@@ -188,6 +188,24 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def fp64_errors(Hd, Ha, Hr, phi, W, w, loss, gW, gphi):
+    """Error of one objective evaluation (loss, dL/dW, dL/dphi from the GPU)
+    against the FP64 oracle on the same channels: relative error of the loss
+    and max-abs error of each gradient over the gradient's largest entry.
+    Run after the timed region; the oracle is the checker here."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import objective_oracle as OO
+    c = lambda t: t.detach().cpu().numpy()
+    C = W.shape[0]
+    lo, gWo, gpo = OO.objective_from_weights(c(Hd), c(Ha), c(Hr), c(phi), c(W), w,
+                                             np.zeros(C, bool))
+    g1, g2 = c(gW).reshape(gWo.shape), c(gphi)
+    return {"loss": abs(float(loss) - lo) / abs(lo),
+            "grad_W": float(np.abs(g1 - gWo).max() / np.abs(gWo).max()),
+            "grad_phi": float(np.abs(g2 - gpo).max() / np.abs(gpo).max()),
+            "vs": "FP64 oracle, same channels, one evaluation"}
+
+
 def objective_bench(torch, steps, flush, cpu_baseline=False):
     """Plain objective fwd+bwd, S=16 M=1024 R=4096 C=1, through the C ABI.
 
@@ -266,6 +284,8 @@ def objective_bench(torch, steps, flush, cpu_baseline=False):
     reps = max(1, steps // NSET)
     t = timed(ev_plan, reps)
     loss_plan = loss.clone()
+    st.synchronize()
+    err = fp64_errors(*sets[0], phi, W, 1.0 / R, loss[0], gW[0], gphi[0])
     t_direct = timed(ev_direct, reps)
     rel = float(((loss_plan - loss).abs() / loss.abs()).max())
     for h in plans:
@@ -301,6 +321,7 @@ def objective_bench(torch, steps, flush, cpu_baseline=False):
                        "plan_create_ms": t_plan * 1e3},
             "direct_call": {"value": 1e3 / t_direct, "ms_per_eval": t_direct,
                             "max_rel_loss_diff": rel},
+            "rel_err_vs_fp64": err,
             "cpu_baseline": cpu,
             "roofline": {"bound": "hbm", "kernel": "k_obj_stream_t", "achieved": achieved,
                          "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -379,6 +400,8 @@ def objective_codes_bench(torch, R=4096, C=60, nset=4, reps=20):
         return e0.elapsed_time(e1) / (n * nset)
     t_tc = timed(ev_tc, reps)
     loss_tc = loss.clone()
+    st.synchronize()
+    err = fp64_errors(*sets[0], phi, W, 1.0 / R, loss[0], gW[0], gphi[0])
     t_cc = timed(ev_cc, max(2, reps // 4))
     rel = float(((loss_tc - loss).abs() / loss.abs()).max())
     K = M + S
@@ -407,6 +430,7 @@ def objective_codes_bench(torch, R=4096, C=60, nset=4, reps=20):
                              "plan operands), CUDA-graph replay"},
             "cuda_core_path": {"value": 1e3 / t_cc, "ms_per_eval": t_cc},
             "speedup_vs_cuda_core": t_cc / t_tc,
+            "rel_err_vs_fp64": err,
             "max_rel_loss_diff_vs_cuda_core": rel,
             "algorithmic_tflops": alg_flop / (t_tc * 1e-3) / 1e12,
             "roofline": {"bound": "hbm", "kernel": "k_cgemm3 (both GEMMs)", "achieved": gbs,
@@ -481,20 +505,20 @@ def batch_bench(torch, n_place=64, workers=4, opt_steps=20):
     placement.batch_evaluate(cfg, [small], workers=1, opt_steps=2)
     res, wall = placement.batch_evaluate(cfg, list(range(n_place)), workers=workers,
                                          opt_steps=opt_steps)
-    sizes = sorted({r["size"] for r in res})
-    by_size = {str(n): {"count": sum(1 for r in res if r["size"] == n),
-                        "mean_trace_s": float(np.mean([r["t_trace"] for r in res if r["size"] == n])),
-                        "mean_opt_s": float(np.mean([r["t_opt"] for r in res if r["size"] == n]))}
-               for n in sizes}
     paths = sum(r["rx_paths"] for r in res)
     improved = sum(1 for r in res if r["loss_last"] < r["loss_first"])
+    gain = [r["loss_first"] - r["loss_last"] for r in res]
     return {"metric": "batched hyper-configs/s (trace + objective+adjoint)", "value": n_place / wall,
             "unit": "configs/s", "wall_s": wall, "rx_paths_per_s": paths / wall,
             "config": {"workload": "multi-room building, 199,976 triangles, 16-element AP, "
                                    "256x256 Rx, 1000x1000 launch, 2 reflections",
                        "placements": n_place, "sizes": "16x16 to 64x64 (step 8)",
                        "workers": workers, "adam_steps": opt_steps},
-            "by_size": by_size, "placements_with_lower_loss": improved}
+            "mean_trace_s": float(np.mean([r["t_trace"] for r in res])),
+            "mean_opt_s": float(np.mean([r["t_opt"] for r in res])),
+            "placements_with_lower_loss": improved,
+            "median_loss_decrease": float(np.median(gain)),
+            "median_ms_share": float(np.median([r["ms_share"] for r in res]))}
 
 
 def channel_ms_bench(torch, warmup, steps, flush):
@@ -540,10 +564,8 @@ def channel_ms_bench(torch, warmup, steps, flush):
     for key, v in per.items():
         ms = sum(a for a, _ in v) / len(v)
         st = v[0][1]
-        traces[key] = {"ms": ms, "rx_paths": st["rx_paths"], "tasks": st["tasks"],
-                       "unique_paths": st["unique_paths"], "rounds": st["rounds"],
-                       "ms_stage1": st["ms_stage1"], "ms_stage2": st["ms_stage2"],
-                       "segments_fwd": st["segments_fwd"], "segments_bwd": st["segments_bwd"]}
+        traces[key] = {"ms": round(ms, 2), "rx_paths": st["rx_paths"],
+                       "ms_stage2": round(st["ms_stage2"], 2)}
         tot_ms += ms
         tot_paths += st["rx_paths"]
     # objective + adjoint on the traced channels, reference orientation
@@ -573,6 +595,8 @@ def channel_ms_bench(torch, warmup, steps, flush):
     e1.record(stream)
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / n_ev
+    torch.cuda.synchronize()
+    err = fp64_errors(Hd, Ha, Hr, phi, W, 1.0 / R, loss[0], gW, gphi)
     bytes_alg = 8 * (R * M + M * S + R * S)
     hbm, kind = peaks()
     achieved = bytes_alg / (t * 1e-3) / 1e9
@@ -588,7 +612,7 @@ def channel_ms_bench(torch, warmup, steps, flush):
                           "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
                                        "unit": "GB/s", "frac": achieved / hbm,
                                        "algorithmic_bytes": bytes_alg, "peak_kind": kind},
-                          "loss": float(loss)}}
+                          "loss": float(loss), "rel_err_vs_fp64": err}}
 
 
 def main():
@@ -748,7 +772,8 @@ def main():
     k1_ms = st0["ms_stage1"]
     succ = st0["rx_paths"]
     sm_mhz = clocks["sm_mhz"] or 2070.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * sm_mhz * 1e6 / 1e12
     # stage 1 (the dominant kernel): algorithmic output = the reference's
     # forward records (60 B each); work = ideal-BVH flop per query
     alg1 = RECORD_BYTES * st0["fwd_records"]
@@ -787,7 +812,7 @@ def main():
                          "peak": fp32_peak, "unit": "TFLOP/s", "frac": tfl1 / fp32_peak,
                          "flop_per_segment": FLOP_PER_SEGMENT_FWD,
                          "segments": st0["segments_fwd"],
-                         "peak_kind": "152 SM x 128 lanes x 2 at the sampled SM clock"},
+                         "peak_kind": f"{n_sm} SM x 128 lanes x 2 at the sampled SM clock"},
         "roofline_stage2": {"bound": "hbm", "kernel": "k_stage2", "achieved": gbs2, "peak": hbm,
                             "unit": "GB/s", "frac": gbs2 / hbm, "traffic": stage2_traffic(),
                             "peak_kind": peak_kind, "algorithmic_bytes": alg2},

@@ -188,3 +188,69 @@ def test_non_finite_vertices_rejected(tracer):
     _, st = sc.trace(c["src"], c["dst"], c["params"])
     assert st["rx_paths"] > 0
     sc.close()
+
+
+def _ms256_reduced(key):
+    """The 50,028-triangle room of the ms-256 channel set with a reduced
+    launch (200 x 200), a 32x32 Rx grid and a 6x6 metasurface, 3 reflections:
+    AP->Rx with the metasurface's blackhole quad, AP->MS (beam types 2 -> 1)
+    and MS->Rx (1 -> 0)."""
+    from automs_gb300 import scenes
+    cfg = scenes.channel_ms_config("ms-256")
+    lam = scenes.WAVE_LEN_60GHZ
+    pos, quad, _ = scenes.metasurface((6.0, 8.0 - 1e-3, 2.0), (0, -1, 0), (0, 0, -1), 6, lam / 2)
+    dst = scenes.rx_grid(0.25, 11.75, 32, 0.25, 7.75, 32, 1.5)
+    t = cfg["traces"][key]
+    p = dict(t["params"], launch_x=200, launch_y=200)
+    tris, mat, mp = cfg["tris"], cfg["mat"], cfg["mat_prop"]
+    if key == "src_to_dst":
+        tris, mat, mp = scenes.with_blackholes(tris, mat, mp, [quad])
+        src, d = t["src"], dst
+    elif key == "src_to_ms{0}":
+        src, d = t["src"], pos
+    else:
+        src, d = pos, dst
+    return dict(tris=tris, mat=mat, mat_prop=mp, src=src, dst=d, params=p)
+
+
+def _exact_parity(tracer, c, power_db=0.1):
+    H, st, paths = run_gpu(tracer, c)
+    Ho, so, po = oracle.trace_channel(c["tris"], c["mat"], c["mat_prop"], c["src"], c["dst"],
+                                      c["params"])
+    for k in cases.STAT_KEYS + ("tasks", "overflow"):
+        assert st[k] == so[k], (k, st[k], so[k])
+    assert so["rx_paths"] > 0
+    assert np.array_equal(paths, po)
+    assert np.array_equal(H != 0, Ho != 0)
+    assert rel(H, Ho) < 1e-5
+    pw, po_ = np.abs(H.sum(0)) ** 2, np.abs(Ho.sum(0)) ** 2
+    m = po_ > 0
+    assert np.abs(10 * np.log10(pw[m] / po_[m])).max() < power_db
+    return st
+
+
+@pytest.mark.parametrize("key", ["src_to_dst", "src_to_ms{0}", "ms{0}_to_dst"])
+def test_sah_scene_channel_set_parity_with_oracle(tracer, key):
+    """Scenes of 16,384+ triangles take the binned-SAH hierarchy built on
+    the host (50,028 triangles here): every trace of a one-metasurface
+    channel set equals the oracle bit for bit on counters and paths, H to
+    1e-5 and per-Rx power to 0.1 dB."""
+    c = _ms256_reduced(key)
+    assert c["tris"].shape[0] >= 16384
+    _exact_parity(tracer, c)
+
+
+@pytest.mark.parametrize("L", [2, 3])
+def test_building_sah_parity_with_oracle(tracer, L):
+    """A six-room building (3 x 2 rooms with door gaps and furniture,
+    19,886 triangles: the SAH hierarchy) traced exactly as the oracle does."""
+    from automs_gb300 import scenes
+    tris, mat, mp, xs, ys = scenes.multiroom_scene(20_000, rooms=(3, 2), seed=5)
+    assert tris.shape[0] >= 16384
+    lam = scenes.WAVE_LEN_60GHZ
+    src = scenes.ula(((xs[1] + xs[2]) / 2, (ys[0] + ys[1]) / 2, 2.5), (1, 0, 0), 4, lam / 2)
+    dst = scenes.rx_grid(0.25, xs[-1] - 0.25, 48, 0.25, ys[-1] - 0.25, 40, 1.5)
+    p = dict(samples_per_launch=1, launch_x=256, launch_y=256, wave_len=lam, max_reflection=L,
+             reserve_size=100, src_bptype=2, dst_bptype=0, dst_gridsize=5, src_r=0.5e-5,
+             dst_r=0.06, src_dir=[0.0, 1.0, 0.0], dst_dir=[0.0, 0.0, 0.0])
+    _exact_parity(tracer, dict(tris=tris, mat=mat, mat_prop=mp, src=src, dst=dst, params=p))
