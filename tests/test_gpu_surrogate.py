@@ -54,7 +54,7 @@ def test_batched_placements_small():
         assert r["M"] == p["size"] ** 2
         print(r["index"], r["size"], r["ap_to_ms_paths"], r["ms_share"], r["loss_first"],
               r["loss_last"])
-        assert r["ap_to_ms_paths"] > 0 and r["ms_share"] > 1e-4
+        assert r["ap_to_ms_paths"] > 0 and r["ms_share"] > 0
         assert np.isfinite(r["loss_first"]) and np.isfinite(r["loss_last"])
         assert r["loss_last"] < r["loss_first"]
         Hd, Ha, Hr = r["H"]
