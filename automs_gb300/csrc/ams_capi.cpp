@@ -393,7 +393,7 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     need += al(lbvh_output_bytes(n_src)) + al(lbvh_output_bytes(n_dst));
     need += al(8 * (size_t)tab_size) + al(56 * (size_t)tab_size);
     need += 3 * al(4 * (size_t)ng * W);
-    need += al(4 * ((size_t)ng + 1)) + al(4 * (size_t)ng) + al(8 * ((size_t)ng + 1)) + al(4);
+    need += 2 * al(4 * ((size_t)ng + 1)) + 2 * al(4 * (size_t)tab_size);
     need += al(16 * (size_t)n_src * n_dst);
     need += al(8 * 16) + al(4);
     need += 4096;
@@ -412,9 +412,9 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     P.N = S->ws.take<unsigned>((size_t)ng * W);
     P.S = S->ws.take<unsigned>((size_t)ng * W);
     P.cell_off = S->ws.take<int>((size_t)ng + 1);
-    P.act_cells = S->ws.take<int>((size_t)ng);
-    P.item_off = S->ws.take<long long>((size_t)ng + 1);
-    P.n_act = S->ws.take<int>(1);
+    P.chunk_off = S->ws.take<int>((size_t)ng + 1);
+    P.slot_of = S->ws.take<int>(tab_size);
+    int *dense_of = S->ws.take<int>(tab_size);
     P.acc = S->ws.take<unsigned long long>(2 * (size_t)n_src * n_dst);
     P.ctr = S->ws.take<unsigned long long>(16);
     P.err = S->ws.take<unsigned>(1);
@@ -483,14 +483,25 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     float ms_k2 = 0.f;
     unsigned long long n_new = unique_records;
     if (fwd_records > 0) {
-      CK(cudaMemcpyAsync(P.N, P.T, 4 * (size_t)ng * W, cudaMemcpyDeviceToDevice, st));
+      // stage 2 on dense path ids: the bitmaps shrink from one bit per table
+      // slot to one per path found
+      P.n_paths = (int)n_paths;
+      P.W = (int)((n_paths + 31) / 32);
+      const size_t dwords = (size_t)ng * P.W;
+      CK(cudaMemsetAsync(P.N, 0, 4 * dwords, st));
+      CK(trace_dense_paths(P, P.T, W, dense_of, P.N, st));
+      CK(cudaMemcpyAsync(P.T, P.N, 4 * dwords, cudaMemcpyDeviceToDevice, st));
+      CK(cudaMemsetAsync(P.S, 0, 4 * dwords, st));
       while (n_new > 0) {
-        if (S->tasks.cap < n_new * sizeof(int)) {
+        // per task: its path id and at most one chunk record
+        const size_t per_task = sizeof(int) + sizeof(int2);
+        if (S->tasks.cap < n_new * per_task + 512) {
           CK(cudaStreamSynchronize(st));
-          CK(S->tasks.ensure(std::max<size_t>(n_new * sizeof(int) * 2, 1 << 20)));
+          CK(S->tasks.ensure(std::max<size_t>(n_new * per_task * 2 + 512, 1 << 20)));
         }
-        P.task_slot = reinterpret_cast<int *>(S->tasks.base);
-        P.task_cap = S->tasks.cap / sizeof(int);
+        P.task_cap = (S->tasks.cap - 512) / per_task;
+        P.task_path = reinterpret_cast<int *>(S->tasks.base);
+        P.chunk_at = reinterpret_cast<int2 *>(S->tasks.base + al(sizeof(int) * P.task_cap));
         P.kpi = trace_paths_per_item(P, n_new);
         CK(cudaMemsetAsync(P.ctr + 5, 0, 8, st));
         CK(cudaMemsetAsync(P.ctr + 7, 0, 8, st));

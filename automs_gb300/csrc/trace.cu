@@ -565,7 +565,7 @@ struct S1Ray {
 // the hit of the finished query (stage-1 closest-hit program,
 // optixPathTracer.cu:285-331)
 __device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, Slot *slots,
-                                    const CurMatrix &cm, int *rec,
+                                    const CurMatrix &cm, volatile int *los_slot, int *rec,
                                     unsigned long long &my_records) {
   const int L = P.L;
   if (q.best.inst == 3) { w.ttl = 0; return; }
@@ -617,14 +617,19 @@ __device__ __forceinline__ void s1_hit(const TraceDev &P, S1Query &q, S1Ray &w, 
         rec[w.res_cnt++] = cell * 8 + hc;
         int slot = w.key_slot;
         if (w.key_cur != w.cur || w.key_ttl != w.ttl) {
-          int32_t key[14];
+          // the primary ray's key depends on the hit count only (identity
+          // matrix, slot 0), so the CTA keeps its slot per hit count
+          slot = w.cur == 0 ? los_slot[hc] : -1;
+          if (slot < 0) {
+            int32_t key[14];
+            const Mat34 M = cm.get(w.cur);
 #pragma unroll
-          const Mat34 M = cm.get(w.cur);
-#pragma unroll
-          for (int k = 0; k < 12; k++) key[k] = fbits(M.m[k]);
-          key[12] = hc;
-          key[13] = w.cur;
-          slot = path_insert(P, key);
+            for (int k = 0; k < 12; k++) key[k] = fbits(M.m[k]);
+            key[12] = hc;
+            key[13] = w.cur;
+            slot = path_insert(P, key);
+            if (w.cur == 0 && slot >= 0) los_slot[hc] = slot;
+          }
           w.key_cur = w.cur;
           w.key_ttl = w.ttl;
           w.key_slot = slot;
@@ -722,6 +727,10 @@ __global__ void __launch_bounds__(128, 8) k_stage1(TraceDev P) {
   unsigned long long my_records = 0, my_segs = 0, my_capped = 0;
   __shared__ float s_curm[12 * 128];
   const CurMatrix cm{s_curm};
+  // path-table slot of the primary ray's key per hit count (-1: not known)
+  __shared__ int s_los[AMS_MAX_L + 2];
+  if (threadIdx.x < AMS_MAX_L + 2) s_los[threadIdx.x] = -1;
+  __syncthreads();
   int rec[AMS_MAX_RESERVE];  // cell * 8 + hit_cnt of the records kept so far
   Slot slots[1 << LMAX];     // deferred branch slots
   int st_node[AMS_STACK];
@@ -808,7 +817,7 @@ __global__ void __launch_bounds__(128, 8) k_stage1(TraceDev P) {
     // ---- hits of the waiting lanes, then their next queries
     if (live && q.phase == PH_HIT) {
       my_segs++;
-      s1_hit(P, q, w, slots, cm, rec, my_records);
+      s1_hit(P, q, w, slots, cm, s_los, rec, my_records);
       live = s1_next(P, q, w, slots, cm, n_fetch, tiles_y, my_capped);
     }
   }
@@ -827,16 +836,43 @@ __global__ void __launch_bounds__(128, 8) k_stage1(TraceDev P) {
 }
 
 // --------------------------------------------------------------- tasks
-// The round's tasks, listed per cell: cell c's new paths are task_slot[
-// cell_off[c] .. cell_off[c + 1]) in increasing slot order; the cells with at
-// least one are act_cells[0 .. n_act), and active cell a owns the stage-2
-// items item_off[a] .. item_off[a + 1): ceil(paths / kpi) path chunks times
-// G groups of 32 (Rx, Tx) pairs.  A warp per cell counts, one CTA scans, a
-// warp per cell fills.
-__device__ __forceinline__ long long s2_groups(const TraceDev &P) {
-  return ((long long)P.gs * P.gs * P.n_src + 31) / 32;
+// Dense path ids: after stage 1 the path table is final, so stage 2 numbers
+// its paths 0 .. n_paths - 1 (slot_of maps back to the table) and keeps its
+// bitmaps [cell][W] with W = ceil(n_paths / 32) words instead of one bit per
+// table slot.  The numbering follows the order in which threads claim ids;
+// nothing computed depends on it (sums are exact, lists are per cell).
+__global__ void k_dense_ids(TraceDev P, int *dense_of, unsigned long long *n) {
+  for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s <= P.tab_mask;
+       s += gridDim.x * blockDim.x) {
+    if (P.tab_h[s] == 0ull) continue;
+    const unsigned long long id = atomicAdd(n, 1ull);
+    dense_of[s] = (int)id;
+    P.slot_of[id] = (int)s;
+  }
 }
 
+// out[cell][dense id] = the bits of in[cell][slot] (out zeroed before)
+__global__ void k_to_dense(TraceDev P, const unsigned *in, int w_in, const int *dense_of,
+                           unsigned *out) {
+  const long long nwords = (long long)P.ng * w_in;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nwords;
+       i += (long long)gridDim.x * blockDim.x) {
+    unsigned b = in[i];
+    if (!b) continue;
+    const int cell = (int)(i / w_in), w = (int)(i % w_in);
+    while (b) {
+      const int k = __ffs(b) - 1;
+      b &= b - 1u;
+      const int d = dense_of[w * 32 + k];
+      atomicOr(out + (size_t)cell * P.W + (d >> 5), 1u << (d & 31));
+    }
+  }
+}
+
+// The round's tasks, listed per cell: cell c's new paths (dense ids) are
+// task_path[cell_off[c] .. cell_off[c + 1]) in increasing order, cut into
+// chunks of up to kpi paths: chunk_at[chunk_off[c] ..] = (cell, first
+// task).  A warp per cell counts, one CTA scans, a warp per cell fills.
 __global__ void k_cell_counts(TraceDev P, const unsigned *bits) {
   const int lane = threadIdx.x & 31;
   const int nwarp = (gridDim.x * blockDim.x) >> 5;
@@ -849,59 +885,45 @@ __global__ void k_cell_counts(TraceDev P, const unsigned *bits) {
   }
 }
 
-// exclusive scan of the counts in place (cell_off[ng] = total), the active
-// cell list with its item offsets; one CTA of 1024 threads
+// exclusive scans of the task and chunk counts in place (cell_off[ng] and
+// chunk_off[ng] = totals); one CTA of 1024 threads
 __global__ void __launch_bounds__(1024) k_cell_scan(TraceDev P) {
-  __shared__ long long wsum[32], wits[32];
-  __shared__ int wact[32];
-  __shared__ long long carry_s, icarry_s;
-  __shared__ int act_s;
+  __shared__ int wsum[32], wch[32];
+  __shared__ int carry_s, ccarry_s;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  const long long G = s2_groups(P);
-  if (t == 0) { carry_s = 0; icarry_s = 0; act_s = 0; }
+  if (t == 0) { carry_s = 0; ccarry_s = 0; }
   __syncthreads();
   for (int base = 0; base < P.ng; base += 1024) {
     const int i = base + t;
-    const long long v = i < P.ng ? P.cell_off[i] : 0;
-    const long long it = (v + P.kpi - 1) / P.kpi * G;  // items of this cell
-    long long x = v, y = it;
+    const int v = i < P.ng ? P.cell_off[i] : 0;
+    const int ch = (v + P.kpi - 1) / P.kpi;
+    int x = v, y = ch;
     for (int o = 1; o < 32; o <<= 1) {
-      const long long x2 = __shfl_up_sync(0xffffffffu, x, o);
-      const long long y2 = __shfl_up_sync(0xffffffffu, y, o);
+      const int x2 = __shfl_up_sync(0xffffffffu, x, o);
+      const int y2 = __shfl_up_sync(0xffffffffu, y, o);
       if (lane >= o) { x += x2; y += y2; }
     }
-    const unsigned act = __ballot_sync(0xffffffffu, v > 0);
-    if (lane == 31) { wsum[wid] = x; wits[wid] = y; }
-    if (lane == 0) wact[wid] = __popc(act);
+    if (lane == 31) { wsum[wid] = x; wch[wid] = y; }
     __syncthreads();
-    long long xb = 0, yb = 0;
-    int ab = 0;
-    for (int k = 0; k < wid; k++) { xb += wsum[k]; yb += wits[k]; ab += wact[k]; }
-    const long long carry = carry_s, icarry = icarry_s;
-    const int acar = act_s;
+    int xb = 0, yb = 0;
+    for (int k = 0; k < wid; k++) { xb += wsum[k]; yb += wch[k]; }
+    const int carry = carry_s, ccarry = ccarry_s;
     if (i < P.ng) {
-      P.cell_off[i] = (int)(carry + xb + x - v);
-      if (v > 0) {
-        const int ai = acar + ab + __popc(act & ((1u << lane) - 1u));
-        P.act_cells[ai] = i;
-        P.item_off[ai] = icarry + yb + y - it;
-      }
+      P.cell_off[i] = carry + xb + x - v;
+      P.chunk_off[i] = ccarry + yb + y - ch;
     }
     __syncthreads();
     if (t == 0) {
-      long long xs = 0, ys = 0;
-      int as = 0;
-      for (int k = 0; k < 32; k++) { xs += wsum[k]; ys += wits[k]; as += wact[k]; }
+      int xs = 0, ys = 0;
+      for (int k = 0; k < 32; k++) { xs += wsum[k]; ys += wch[k]; }
       carry_s = carry + xs;
-      icarry_s = icarry + ys;
-      act_s = acar + as;
+      ccarry_s = ccarry + ys;
     }
     __syncthreads();
   }
   if (t == 0) {
-    P.cell_off[P.ng] = (int)carry_s;
-    P.item_off[act_s] = icarry_s;
-    *P.n_act = act_s;
+    P.cell_off[P.ng] = carry_s;
+    P.chunk_off[P.ng] = ccarry_s;
     P.ctr[5] = (unsigned long long)carry_s;
   }
 }
@@ -910,9 +932,10 @@ __global__ void k_cell_fill(TraceDev P, const unsigned *bits) {
   const int lane = threadIdx.x & 31;
   const int nwarp = (gridDim.x * blockDim.x) >> 5;
   for (int cell = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; cell < P.ng; cell += nwarp) {
+    const int first = P.cell_off[cell], end = P.cell_off[cell + 1];
+    if (first == end) continue;
     const unsigned *row = bits + (size_t)cell * P.W;
-    long long pos = P.cell_off[cell];
-    if (pos == P.cell_off[cell + 1]) continue;
+    long long pos = first;
     for (int w0 = 0; w0 < P.W; w0 += 32) {
       const int w = w0 + lane;
       unsigned b = w < P.W ? row[w] : 0u;
@@ -926,11 +949,16 @@ __global__ void k_cell_fill(TraceDev P, const unsigned *bits) {
       while (b) {
         const int k = __ffs(b) - 1;
         b &= b - 1u;
-        if ((unsigned long long)q < P.task_cap) P.task_slot[q] = w * 32 + k;
+        if ((unsigned long long)q < P.task_cap) P.task_path[q] = w * 32 + k;
         else atomicOr(P.err, AMS_DERR_TASKS);
         q++;
       }
       pos += __shfl_sync(0xffffffffu, x, 31);
+    }
+    const int c0 = P.chunk_off[cell], c1 = P.chunk_off[cell + 1];
+    for (int j = c0 + lane; j < c1; j += 32) {
+      if ((unsigned long long)j < P.task_cap) P.chunk_at[j] = make_int2(cell, first + (j - c0) * P.kpi);
+      else atomicOr(P.err, AMS_DERR_TASKS);
     }
   }
 }
@@ -1023,9 +1051,9 @@ __device__ __forceinline__ bool s2_ray(const TraceDev &P, int slot, int s, af3 o
   return ok;
 }
 
-// Persistent stage 2: a warp takes an item = (active cell, a chunk of up to
-// kpi of the cell's new paths, 32 consecutive (Rx within the cell, Tx)
-// pairs, Tx fastest) and traces the chunk's paths one after the other; each
+// Persistent stage 2: a warp takes an item = (a chunk of up to kpi of one
+// cell's new paths, 32 consecutive (Rx within the cell, Tx) pairs, Tx
+// fastest) and traces the chunk's paths one after the other; each
 // lane sums its pair's contributions over the chunk in registers (exact
 // 64-bit fixed point) and adds them once into the Rx-major accumulator
 // acc[dst][s], so a warp's adds cover one or a few contiguous runs of Tx
@@ -1038,8 +1066,7 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
   const int S = P.n_src;
   const long long pairs = (long long)P.gs * P.gs * S;
   const long long G = (pairs + 31) / 32;
-  const int n_act = *P.n_act;
-  const long long n_items = P.item_off[n_act];
+  const long long n_items = (long long)P.chunk_off[P.ng] * G;
   const int lane = threadIdx.x & 31;
   const af3 srcdir = mk3(P.src_dir[0], P.src_dir[1], P.src_dir[2]);
   const af3 dstdir = mk3(P.dst_dir[0], P.dst_dir[1], P.dst_dir[2]);
@@ -1049,21 +1076,19 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
     if (lane == 0) item = atomicAdd(P.ctr + 11, 1ull);
     item = __shfl_sync(0xffffffffu, item, 0);
     if ((long long)item >= n_items) break;
-    // the active cell whose item range holds `item` (binary search)
-    int lo = 0, hi = n_act - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(P.item_off + mid) <= (long long)item) lo = mid; else hi = mid - 1;
-    }
-    const long long local = (long long)item - __ldg(P.item_off + lo);
-    const int cell = __ldg(P.act_cells + lo);
-    const int c0 = __ldg(P.cell_off + cell), c1 = __ldg(P.cell_off + cell + 1);
-    if (c0 < 0 || c1 < c0 || (unsigned long long)c1 > P.task_cap) {
+    const int2 chunk = __ldg(P.chunk_at + item / G);
+    const int cell = chunk.x;
+    if ((unsigned)cell >= (unsigned)P.ng) {
       if (lane == 0) atomicOr(P.err, AMS_DERR_TASKS);
       continue;
     }
-    const int t0 = c0 + (int)(local / G) * P.kpi, t1 = min(c1, t0 + P.kpi);
-    const long long pr = (local % G) * 32 + lane;
+    const int c1 = __ldg(P.cell_off + cell + 1);
+    const int t0 = chunk.y, t1 = min(c1, t0 + P.kpi);
+    if (t0 < 0 || t1 < t0 || (unsigned long long)t1 > P.task_cap) {
+      if (lane == 0) atomicOr(P.err, AMS_DERR_TASKS);
+      continue;
+    }
+    const long long pr = (long long)(item % G) * 32 + lane;
     bool act = pr < pairs;
     const int inner = act ? (int)(pr / S) : 0, s = act ? (int)(pr % S) : 0;
     const int gi = cell / P.n1g, gj = cell % P.n1g;
@@ -1074,7 +1099,8 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
     unsigned long long sre = 0, sim = 0;
     unsigned segs = 0;
     for (int t = t0; t < t1; t++) {
-      const int slot = __ldg(P.task_slot + t);
+      const int path = __ldg(P.task_path + t);
+      const int slot = (unsigned)path < (unsigned)P.n_paths ? __ldg(P.slot_of + path) : -1;
       if ((unsigned)slot > P.tab_mask) {
         if (lane == 0) atomicOr(P.err, AMS_DERR_TASKS);
         break;
@@ -1086,7 +1112,7 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
         if (ok) { sre += cre; sim += cim; n_ok++; } else { n_fail++; }
       }
       if (__any_sync(0xffffffffu, ok) && lane == 0)
-        atomicOr(P.S + (size_t)cell * P.W + (slot >> 5), 1u << (slot & 31));
+        atomicOr(P.S + (size_t)cell * P.W + (path >> 5), 1u << (path & 31));
     }
     n_segs += segs;
     if (act && (sre | sim)) {
@@ -1246,6 +1272,14 @@ int trace_paths_per_item(const TraceDev &P, unsigned long long n_tasks) {
   if (k < 1) k = 1;
   if (k > 16) k = 16;
   return (int)k;
+}
+
+cudaError_t trace_dense_paths(const TraceDev &P, const unsigned *T_slots, int w_slots,
+                              int *dense_of, unsigned *out, cudaStream_t st) {
+  k_dense_ids<<<grid_for((long long)P.tab_mask + 1, 256), 256, 0, st>>>(P, dense_of, P.ctr + 12);
+  k_to_dense<<<grid_for((long long)P.ng * w_slots, 256), 256, 0, st>>>(P, T_slots, w_slots,
+                                                                      dense_of, out);
+  return cudaGetLastError();
 }
 
 cudaError_t trace_make_tasks(const TraceDev &P, const unsigned *bits, cudaStream_t st) {

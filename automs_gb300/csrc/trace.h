@@ -48,32 +48,39 @@ struct TraceDev {
   int32_t *tab_key;  // 14 words per slot, sign bits flipped (0 = not written yet)
   unsigned tab_mask;
   unsigned tab_limit;  // occupied slots above this -> grow and retry
-  // task bitmaps [ng][W] in slot space
+  // task bitmaps [ng][W]: stage 1 sets T in table-slot space (W = slots /
+  // 32); stage 2 runs on dense path ids (W = ceil(n_paths / 32))
   unsigned *T;  // traced
   unsigned *N;  // new this round
   unsigned *S;  // succeeded this round
   int W;
-  // tasks of the current round per cell: slots task_slot[cell_off[c] ..
-  // cell_off[c + 1]) of cell c; cells with tasks act_cells[0 .. *n_act),
-  // active cell a owning stage-2 items item_off[a] .. item_off[a + 1)
-  int *task_slot;
-  unsigned long long task_cap;
-  int *cell_off;        // [ng + 1]
-  int *act_cells;       // [ng]
-  long long *item_off;  // [ng + 1]
-  int *n_act;
-  int kpi;              // paths per stage-2 item this round
+  // stage-2 path ids: dense id -> table slot
+  int *slot_of;
+  int n_paths;
+  // tasks of the current round per cell: dense path ids task_path[cell_off[c]
+  // .. cell_off[c + 1]) of cell c, cut into chunks of up to kpi paths,
+  // chunk_at[chunk_off[c] .. chunk_off[c + 1]) = (cell, first task)
+  int *task_path;
+  int2 *chunk_at;
+  unsigned long long task_cap;  // entries of task_path and of chunk_at
+  int *cell_off;   // [ng + 1]
+  int *chunk_off;  // [ng + 1]
+  int kpi;         // paths per stage-2 item this round
   // fixed-point channel accumulators, Rx-major: acc[(dst * n_src + s) * 2]
   unsigned long long *acc;
   // counters: 0 records, 1 overflow threads, 2 occupied slots, 3 ok rays,
   // 4 failed rays, 5 tasks this round, 6 unique records, 7 new tasks,
   // 8 stage-1 closest-hit queries, 9 stage-2 closest-hit queries,
-  // 10 stage-1 launch-index fetch, 11 stage-2 item fetch
+  // 10 stage-1 launch-index fetch, 11 stage-2 item fetch, 12 dense path ids
   unsigned long long *ctr;
   unsigned *err;
 };
 
 cudaError_t trace_stage1(const TraceDev &P, cudaStream_t st);
+// dense path ids (dense_of [slots], P.slot_of) and the stage-1 bitmap
+// T_slots [ng][w_slots] turned into dense ids in `out` [ng][P.W], zeroed before
+cudaError_t trace_dense_paths(const TraceDev &P, const unsigned *T_slots, int w_slots,
+                              int *dense_of, unsigned *out, cudaStream_t st);
 // paths per stage-2 item for a round of n_tasks tasks (set P.kpi before
 // listing the round's tasks)
 int trace_paths_per_item(const TraceDev &P, unsigned long long n_tasks);
