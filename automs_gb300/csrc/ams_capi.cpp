@@ -393,7 +393,7 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     need += al(lbvh_output_bytes(n_src)) + al(lbvh_output_bytes(n_dst));
     need += al(8 * (size_t)tab_size) + al(56 * (size_t)tab_size);
     need += 3 * al(4 * (size_t)ng * W);
-    need += 2 * al(4 * ((size_t)ng + 1)) + 2 * al(4 * (size_t)tab_size);
+    need += 2 * al(4 * ((size_t)ng + 1)) + al(4 * (size_t)ng) + 2 * al(4 * (size_t)tab_size);
     need += al(16 * (size_t)n_src * n_dst);
     need += al(8 * 16) + al(4);
     need += 4096;
@@ -413,6 +413,7 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     P.S = S->ws.take<unsigned>((size_t)ng * W);
     P.cell_off = S->ws.take<int>((size_t)ng + 1);
     P.chunk_off = S->ws.take<int>((size_t)ng + 1);
+    P.cell_cnt = S->ws.take<int>((size_t)ng);
     P.slot_of = S->ws.take<int>(tab_size);
     int *dense_of = S->ws.take<int>(tab_size);
     P.acc = S->ws.take<unsigned long long>(2 * (size_t)n_src * n_dst);
@@ -491,21 +492,18 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
       CK(cudaMemsetAsync(P.N, 0, 4 * dwords, st));
       CK(trace_dense_paths(P, P.T, W, dense_of, P.N, st));
       CK(cudaMemcpyAsync(P.T, P.N, 4 * dwords, cudaMemcpyDeviceToDevice, st));
-      CK(cudaMemsetAsync(P.S, 0, 4 * dwords, st));
+      CK(trace_count_tasks(P, P.N, st));
       while (n_new > 0) {
-        // per task: its path id and at most one chunk record
-        const size_t per_task = sizeof(int) + sizeof(int2);
+        // per task: its (path id, slot) and at most one chunk record
+        const size_t per_task = sizeof(int2) + sizeof(int4);
         if (S->tasks.cap < n_new * per_task + 512) {
           CK(cudaStreamSynchronize(st));
           CK(S->tasks.ensure(std::max<size_t>(n_new * per_task * 2 + 512, 1 << 20)));
         }
         P.task_cap = (S->tasks.cap - 512) / per_task;
-        P.task_path = reinterpret_cast<int *>(S->tasks.base);
-        P.chunk_at = reinterpret_cast<int2 *>(S->tasks.base + al(sizeof(int) * P.task_cap));
+        P.task_path = reinterpret_cast<int2 *>(S->tasks.base);
+        P.chunk_at = reinterpret_cast<int4 *>(S->tasks.base + al(sizeof(int2) * P.task_cap));
         P.kpi = trace_paths_per_item(P, n_new);
-        CK(cudaMemsetAsync(P.ctr + 5, 0, 8, st));
-        CK(cudaMemsetAsync(P.ctr + 7, 0, 8, st));
-        CK(cudaMemsetAsync(P.ctr + 11, 0, 8, st));
         CK(trace_make_tasks(P, P.N, st));
         CK(cudaEventRecord(S->k2[0], st));
         CK(trace_stage2(P, n_new, st));

@@ -59,10 +59,11 @@ struct TraceDev {
   int n_paths;
   // tasks of the current round per cell: dense path ids task_path[cell_off[c]
   // .. cell_off[c + 1]) of cell c, cut into chunks of up to kpi paths,
-  // chunk_at[chunk_off[c] .. chunk_off[c + 1]) = (cell, first task)
-  int *task_path;
-  int2 *chunk_at;
+  // chunk_at[chunk_off[c] .. chunk_off[c + 1])
+  int2 *task_path;  // (dense path id, table slot)
+  int4 *chunk_at;   // (cell, first task, end task, 0)
   unsigned long long task_cap;  // entries of task_path and of chunk_at
+  int *cell_cnt;   // [ng] tasks per cell of the coming round
   int *cell_off;   // [ng + 1]
   int *chunk_off;  // [ng + 1]
   int kpi;         // paths per stage-2 item this round
@@ -71,7 +72,7 @@ struct TraceDev {
   // counters: 0 records, 1 overflow threads, 2 occupied slots, 3 ok rays,
   // 4 failed rays, 5 tasks this round, 6 unique records, 7 new tasks,
   // 8 stage-1 closest-hit queries, 9 stage-2 closest-hit queries,
-  // 10 stage-1 launch-index fetch, 11 stage-2 item fetch, 12 dense path ids
+  // 10 stage-1 launch-index fetch, 12 dense path ids
   unsigned long long *ctr;
   unsigned *err;
 };
@@ -84,6 +85,9 @@ cudaError_t trace_dense_paths(const TraceDev &P, const unsigned *T_slots, int w_
 // paths per stage-2 item for a round of n_tasks tasks (set P.kpi before
 // listing the round's tasks)
 int trace_paths_per_item(const TraceDev &P, unsigned long long n_tasks);
+// tasks per cell of the first stage-2 round (later rounds: trace_expand)
+cudaError_t trace_count_tasks(const TraceDev &P, const unsigned *bits, cudaStream_t st);
+// the round's task and chunk lists; also clears the success bitmap
 cudaError_t trace_make_tasks(const TraceDev &P, const unsigned *bits, cudaStream_t st);
 cudaError_t trace_stage2(const TraceDev &P, unsigned long long n_tasks, cudaStream_t st);
 cudaError_t trace_expand(const TraceDev &P, cudaStream_t st);
