@@ -1071,9 +1071,11 @@ __device__ __forceinline__ bool s2_ray(const TraceDev &P, int slot, int s, af3 o
 // acc[dst][s], so a warp's adds cover one or a few contiguous runs of Tx
 // (coalesced), one atomic add per (Tx, Rx) and chunk instead of two per
 // verified ray.  The lanes of an item trace the same path key from the same
-// Rx to neighbouring Tx elements: nearly identical rays.  Warps take items
-// in a fixed stride (no fetch round trip); kpi is chosen per round by the
-// host so that a round still has several items per resident warp.
+// Rx to neighbouring Tx elements: nearly identical rays.  One warp per item,
+// 8 per CTA: the block scheduler balances items of uneven cost (fixed
+// strides over persistent warps and a fetch counter both measured slower);
+// kpi is chosen per round by the host so that a round keeps several items
+// per resident warp.
 __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
   const int S = P.n_src;
   const long long pairs = (long long)P.gs * P.gs * S;
@@ -1083,15 +1085,17 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
   const af3 srcdir = mk3(P.src_dir[0], P.src_dir[1], P.src_dir[2]);
   const af3 dstdir = mk3(P.dst_dir[0], P.dst_dir[1], P.dst_dir[2]);
   unsigned long long n_ok = 0, n_fail = 0, n_segs = 0;
-  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
-  for (long long item = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-       item < n_items; item += nwarps) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n_items > (long long)gridDim.x * (blockDim.x >> 5))
+    atomicOr(P.err, AMS_DERR_TASKS);  // the launch must cover every item
+  {
+    const long long item = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (item >= n_items) return;
     const int4 chunk = __ldg(P.chunk_at + item / G);
     const int cell = chunk.x, t0 = chunk.y, t1 = chunk.z;
     if ((unsigned)cell >= (unsigned)P.ng || t0 < 0 || t1 < t0 ||
         (unsigned long long)t1 > P.task_cap) {
       if (lane == 0) atomicOr(P.err, AMS_DERR_TASKS);
-      continue;
+      return;
     }
     const long long pr = (long long)(item % G) * 32 + lane;
     bool act = pr < pairs;
@@ -1298,14 +1302,16 @@ cudaError_t trace_make_tasks(const TraceDev &P, const unsigned *bits, cudaStream
 
 cudaError_t trace_stage2(const TraceDev &P, unsigned long long n_tasks, cudaStream_t st) {
   if (n_tasks == 0) return cudaSuccess;
-  // persistent: as many CTAs as are resident, fewer for a small round
+  // one warp per item; the chunks number at most n_tasks / kpi + one per
+  // cell (the exact count is on the device, warps beyond it return)
   const unsigned long long pairs = (unsigned long long)(P.gs * P.gs) * P.n_src;
-  const unsigned long long items_max = n_tasks * ((pairs + 31) / 32);
-  long long blocks = (long long)stage2_per_sm() * ams_device_sms();
-  const long long need = (long long)((items_max + 7) / 8);
-  if (blocks > need) blocks = need;
-  if (blocks < 1) blocks = 1;
-  k_stage2<<<(int)blocks, 256, 0, st>>>(P);
+  const unsigned long long k = (unsigned long long)P.kpi;
+  unsigned long long chunks = (n_tasks + k - 1) / k + (unsigned long long)P.ng;
+  if (chunks > n_tasks) chunks = n_tasks;
+  const unsigned long long items_max = chunks * ((pairs + 31) / 32);
+  const unsigned long long blocks = (items_max + 7) / 8;
+  if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+  k_stage2<<<(unsigned)blocks, 256, 0, st>>>(P);
   return cudaGetLastError();
 }
 

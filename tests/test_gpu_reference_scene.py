@@ -78,8 +78,11 @@ def test_build_channels_on_reference_scene(tmp_path):
         Ho, so, po = oracle.trace_channel(t, mt, mp, src, dst, p)
         assert np.array_equal(paths, po), key
         assert np.linalg.norm(H - Ho) / np.linalg.norm(Ho) < 1e-5, key
-    # every trace but AP -> ms1 (the relay faces away from the AP: the
-    # reference's "No path found!" case, all zeros on both sides) has paths,
-    # the metasurface-to-metasurface trace (beam types 1 -> 1) included
-    assert with_paths == len(ch) - 1
+    # the traces with a non-zero channel are the reference's (AP -> ms1 finds
+    # no path, "No path found!"; AP -> ms0 verifies rays that arrive outside
+    # the metasurface's receive lobe, with zero amplitude), and they include
+    # the metasurface-to-metasurface trace (beam types 1 -> 1)
+    nonzero = [k for k in fx["keys"]
+               if np.abs(fx[str(k).replace("{", "").replace("}", "") + "_H"]).max() > 0]
+    assert with_paths == len(nonzero) >= 3
     assert np.abs(fx["ms0_to_ms1_H"]).max() > 0
