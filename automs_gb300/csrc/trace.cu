@@ -1084,7 +1084,7 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
   const int lane = threadIdx.x & 31;
   const af3 srcdir = mk3(P.src_dir[0], P.src_dir[1], P.src_dir[2]);
   const af3 dstdir = mk3(P.dst_dir[0], P.dst_dir[1], P.dst_dir[2]);
-  unsigned long long n_ok = 0, n_fail = 0, n_segs = 0;
+  unsigned n_ok = 0, n_fail = 0, n_segs = 0;
   if (blockIdx.x == 0 && threadIdx.x == 0 && n_items > (long long)gridDim.x * (blockDim.x >> 5))
     atomicOr(P.err, AMS_DERR_TASKS);  // the launch must cover every item
   {
@@ -1104,9 +1104,7 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
     const int di = inner / P.gs + gi * P.gs, dj = inner % P.gs + gj * P.gs;
     const int dst = di * P.n1_dst + dj;
     if (dst >= P.n_dst || (P.strict_grid && (di >= P.n0_dst || dj >= P.n1_dst))) act = false;
-    const af3 o = act ? ld3(P.dst + 3 * dst) : mk3(0.f, 0.f, 0.f);
     unsigned long long sre = 0, sim = 0;
-    unsigned segs = 0;
     for (int t = t0; t < t1; t++) {
       const int2 task = __ldg(P.task_path + t);
       const int path = task.x, slot = task.y;
@@ -1117,13 +1115,12 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
       bool ok = false;
       if (act) {
         unsigned long long cre = 0, cim = 0;
-        ok = s2_ray(P, slot, s, o, srcdir, dstdir, segs, cre, cim);
+        ok = s2_ray(P, slot, s, ld3(P.dst + 3 * dst), srcdir, dstdir, n_segs, cre, cim);
         if (ok) { sre += cre; sim += cim; n_ok++; } else { n_fail++; }
       }
       if (__any_sync(0xffffffffu, ok) && lane == 0)
         atomicOr(P.S + (size_t)cell * P.W + (path >> 5), 1u << (path & 31));
     }
-    n_segs += segs;
     if (act && (sre | sim)) {
       unsigned long long *acc = P.acc + ((size_t)dst * S + s) * 2;
       atomicAdd(acc, sre);
@@ -1136,9 +1133,9 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
     n_segs += __shfl_xor_sync(0xffffffffu, n_segs, off);
   }
   if (lane == 0) {
-    if (n_segs) atomicAdd(P.ctr + 9, n_segs);
-    if (n_ok) atomicAdd(P.ctr + 3, n_ok);
-    if (n_fail) atomicAdd(P.ctr + 4, n_fail);
+    if (n_segs) atomicAdd(P.ctr + 9, (unsigned long long)n_segs);
+    if (n_ok) atomicAdd(P.ctr + 3, (unsigned long long)n_ok);
+    if (n_fail) atomicAdd(P.ctr + 4, (unsigned long long)n_fail);
   }
 }
 
