@@ -1139,6 +1139,71 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
   }
 }
 
+// Stage 2 for rounds whose items hold one path each (kpi == 1, where the
+// per-lane sums above have nothing to add up): one thread per backward ray,
+// rays of all tasks laid out back to back (task-major, then Rx within the
+// cell, then Tx), so no warp idles on the padding of a task's last item.
+// Each verified ray adds its contribution to the Rx-major accumulator.
+__global__ void __launch_bounds__(256, 5) k_stage2_rays(TraceDev P) {
+  const int S = P.n_src;
+  const long long pairs = (long long)P.gs * P.gs * S;
+  const long long n_rays = (long long)P.cell_off[P.ng] * pairs;
+  const long long ray = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && n_rays > (long long)gridDim.x * blockDim.x)
+    atomicOr(P.err, AMS_DERR_TASKS);  // the launch must cover every ray
+  if (ray - lane >= n_rays) return;   // the whole warp is past the last ray
+  bool valid = ray < n_rays;
+  const long long t = valid ? ray / pairs : -1;
+  int cell = 0, path = 0, slot = 0, inner = 0, s = 0;
+  if (valid) {
+    const int4 chunk = __ldg(P.chunk_at + t);
+    const int2 task = __ldg(P.task_path + t);
+    cell = chunk.x;
+    path = task.x;
+    slot = task.y;
+    const long long pr = ray % pairs;
+    inner = (int)(pr / S);
+    s = (int)(pr % S);
+    if ((unsigned)cell >= (unsigned)P.ng || (unsigned)path >= (unsigned)P.n_paths ||
+        (unsigned)slot > P.tab_mask || (unsigned long long)t >= P.task_cap) {
+      atomicOr(P.err, AMS_DERR_TASKS);
+      valid = false;
+    }
+  }
+  bool ok = false, traced = false;
+  unsigned segs = 0;
+  if (valid) {
+    const int gi = cell / P.n1g, gj = cell % P.n1g;
+    const int di = inner / P.gs + gi * P.gs, dj = inner % P.gs + gj * P.gs;
+    const int dst = di * P.n1_dst + dj;
+    if (!(dst >= P.n_dst || (P.strict_grid && (di >= P.n0_dst || dj >= P.n1_dst)))) {
+      traced = true;
+      unsigned long long cre = 0, cim = 0;
+      const af3 srcdir = mk3(P.src_dir[0], P.src_dir[1], P.src_dir[2]);
+      const af3 dstdir = mk3(P.dst_dir[0], P.dst_dir[1], P.dst_dir[2]);
+      ok = s2_ray(P, slot, s, ld3(P.dst + 3 * dst), srcdir, dstdir, segs, cre, cim);
+      if (ok) {
+        unsigned long long *acc = P.acc + ((size_t)dst * S + s) * 2;
+        atomicAdd(acc, cre);
+        atomicAdd(acc + 1, cim);
+      }
+    }
+  }
+  // counters and each task's success bit, one atomic per warp / task
+  const unsigned okb = __ballot_sync(0xffffffffu, ok);
+  const unsigned trb = __ballot_sync(0xffffffffu, traced);
+  for (int off = 16; off > 0; off >>= 1) segs += __shfl_xor_sync(0xffffffffu, segs, off);
+  if (lane == 0) {
+    if (segs) atomicAdd(P.ctr + 9, (unsigned long long)segs);
+    if (okb) atomicAdd(P.ctr + 3, (unsigned long long)__popc(okb));
+    if (trb & ~okb) atomicAdd(P.ctr + 4, (unsigned long long)__popc(trb & ~okb));
+  }
+  const unsigned same = __match_any_sync(0xffffffffu, t);
+  if (valid && (okb & same) && lane == __ffs(same) - 1)
+    atomicOr(P.S + (size_t)cell * P.W + (path >> 5), 1u << (path & 31));
+}
+
 // N = (S of the 4 neighbour cells) & ~T; T |= N; S = 0 (cpp:257-300).  The
 // neighbours are linear cell indices +-1 and +-n1g with only the [0, ng)
 // check, exactly as the reference (so row ends wrap).
@@ -1305,6 +1370,12 @@ cudaError_t trace_stage2(const TraceDev &P, unsigned long long n_tasks, cudaStre
   const unsigned long long k = (unsigned long long)P.kpi;
   unsigned long long chunks = (n_tasks + k - 1) / k + (unsigned long long)P.ng;
   if (chunks > n_tasks) chunks = n_tasks;
+  if (P.kpi == 1) {  // one path per item: one thread per ray
+    const unsigned long long blocks = (n_tasks * pairs + 255) / 256;
+    if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+    k_stage2_rays<<<(unsigned)blocks, 256, 0, st>>>(P);
+    return cudaGetLastError();
+  }
   const unsigned long long items_max = chunks * ((pairs + 31) / 32);
   const unsigned long long blocks = (items_max + 7) / 8;
   if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
