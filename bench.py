@@ -596,7 +596,8 @@ def channel_ms_bench(torch, warmup, steps, flush):
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / n_ev
     torch.cuda.synchronize()
-    err = fp64_errors(Hd, Ha, Hr, phi, W, 1.0 / R, loss[0], gW, gphi)
+    err = fp64_errors(*(torch.view_as_complex(x) for x in (Hd, Ha, Hr)), phi, W, 1.0 / R,
+                      loss[0], gW, gphi)
     bytes_alg = 8 * (R * M + M * S + R * S)
     hbm, kind = peaks()
     achieved = bytes_alg / (t * 1e-3) / 1e9
