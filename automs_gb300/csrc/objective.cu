@@ -96,9 +96,12 @@ constexpr int KCHUNK = 256;
 // U[c, m] for the streaming path: 8 lanes per (m, c) split the sum over the
 // AP elements; the dependent streaming kernel may start before this one ends
 // (programmatic dependent launch) and waits for it only before reading U.
-__global__ void __launch_bounds__(256) k_prep_wide(ObjArgs a, int M, float *U) {
+__global__ void __launch_bounds__(256) k_prep_wide(ObjArgs a, int M, float *U, unsigned *err) {
   // let the streaming kernel launch now; it waits for this grid before reading U
   cudaTriggerProgrammaticLaunchCompletion();
+  // the call's wait-timeout word starts clear (a streaming kernel can set it
+  // only after its grid-dependency wait on this grid)
+  if (err && blockIdx.x == 0 && threadIdx.x == 0) *err = 0u;
   const long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 3;
   const int sub = threadIdx.x & 7;
   const bool live = e < (long long)M * a.C;
@@ -122,9 +125,12 @@ __global__ void __launch_bounds__(256) k_prep_wide(ObjArgs a, int M, float *U) {
 
 // U[c, m] = (sum_s W[c, s] H_a[s, m]) e^{j phi'_m}: one thread per (m, c),
 // loads of H_a coalesced over m, issued 8 at a time
-__global__ void __launch_bounds__(128) k_prep(ObjArgs a, int M, float *U) {
+__global__ void __launch_bounds__(128) k_prep(ObjArgs a, int M, float *U, unsigned *err) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
+  // the call's wait-timeout word starts clear (the GEMMs that can set it
+  // run after this kernel)
+  if (err && m == 0 && c == 0) *err = 0u;
   if (m >= M) return;
   c2 v = {0.f, 0.f};
   int s = 0;
@@ -1013,7 +1019,7 @@ cudaError_t run_cb(const ObjArgs &a, const Split &sp, int M, float *U, float *Yp
                    float *gw_part, cudaStream_t st) {
   if (M > 0) {
     dim3 gp((M + 127) / 128, a.C);
-    k_prep<<<gp, 128, 0, st>>>(a, M, U);
+    k_prep<<<gp, 128, 0, st>>>(a, M, U, nullptr);
   }
   dim3 g1((a.R + 31) / 32, sp.kspl);
   k_pass1<CB><<<g1, 256, 0, st>>>(a, M, sp.K, sp.kper, U, Ypart);
@@ -1390,9 +1396,10 @@ cudaError_t run_stream(const ObjArgs &a, const StreamPlan &pl, int M, float *U, 
     return cudaErrorInvalidValue;
   if (M > 0) {
     const long long n = (long long)M * a.C * 8;
-    k_prep_wide<<<(int)((n + 255) / 256), 256, 0, st>>>(a, M, U);
+    k_prep_wide<<<(int)((n + 255) / 256), 256, 0, st>>>(a, M, U, err);
   }
-  cudaError_t e;
+  cudaError_t e = obj_begin_call(err, M > 0, st);
+  if (e != cudaSuccess) return e;
   switch (pl.TR) {
     case 8: e = launch_stream_k<CB, 8>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
     case 4: e = launch_stream_k<CB, 4>(a, pl, mr, md, M, U, Ppart, lpart, err, st); break;
@@ -1867,11 +1874,12 @@ namespace {
 std::atomic<int> g_inject_timeouts{0};
 }  // namespace
 
-// Start of a call on a path with bounded waits: its wait-timeout word is
-// cleared, so the word reports this call only.  An injected timeout (test
-// hook of the error path) sets it right away, as a wait that ran out would.
-cudaError_t obj_begin_call(unsigned *err, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(err, 0, 4, st);
+// Start of a call on a path with bounded waits, after its first kernel: the
+// wait-timeout word is cleared (by that kernel when `cleared`, else here), so
+// the word reports this call only.  An injected timeout (test hook of the
+// error path) then sets it, as a wait that ran out would.
+cudaError_t obj_begin_call(unsigned *err, bool cleared, cudaStream_t st) {
+  cudaError_t e = cleared ? cudaSuccess : cudaMemsetAsync(err, 0, 4, st);
   if (e != cudaSuccess) return e;
   int n = g_inject_timeouts.load();
   while (n > 0 && !g_inject_timeouts.compare_exchange_weak(n, n - 1)) {
@@ -1927,8 +1935,6 @@ cudaError_t obj_run(const ObjArgs &a0, char *scratch, cudaStream_t st) {
     double *lp = reinterpret_cast<double *>(scratch + L.lp);
     unsigned *err = reinterpret_cast<unsigned *>(scratch + L.inv + 48);
     float *GUs = reinterpret_cast<float *>(scratch + L.GUs);
-    cudaError_t e = obj_begin_call(err, st);
-    if (e != cudaSuccess) return e;
     if (cbucket(a.C) == 1) return run_stream<1>(a, pl, M, Um, Pp, lp, GUs, gw, err, counter + 2, st);
     return run_stream<2>(a, pl, M, Um, Pp, lp, GUs, gw, err, counter + 2, st);
   }
@@ -2053,10 +2059,10 @@ cudaError_t run_plan_stream(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st) {
   char *ctl = p->mem + p->oCtl;
   unsigned *counter = reinterpret_cast<unsigned *>(ctl + 40);
   unsigned *err = reinterpret_cast<unsigned *>(ctl + 48);
-  cudaError_t e = obj_begin_call(err, st);
-  if (e != cudaSuccess) return e;
   const long long n = (long long)M * a.C * 8;
-  k_prep_wide<<<(int)((n + 255) / 256), 256, 0, st>>>(a, M, U);
+  k_prep_wide<<<(int)((n + 255) / 256), 256, 0, st>>>(a, M, U, err);
+  cudaError_t e = obj_begin_call(err, true, st);
+  if (e != cudaSuccess) return e;
   switch (p->tTR) {
     case 8: e = launch_stream_ht_k<CB, 8>(p, a, U, Pp, lp, err, st); break;
     case 4: e = launch_stream_ht_k<CB, 4>(p, a, U, Pp, lp, err, st); break;
@@ -2171,11 +2177,11 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
   float *scal = reinterpret_cast<float *>(ctl);
   unsigned *counter = reinterpret_cast<unsigned *>(ctl + 32);
   unsigned *err = reinterpret_cast<unsigned *>(ctl + 48);
+  k_prep<<<dim3((M + 127) / 128, C), 128, 0, st>>>(a, M, U, err);
   {
-    cudaError_t e0 = obj_begin_call(err, st);
+    cudaError_t e0 = obj_begin_call(err, true, st);
     if (e0 != cudaSuccess) return e0;
   }
-  k_prep<<<dim3((M + 127) / 128, C), 128, 0, st>>>(a, M, U);
   const long long nay = (long long)C * (p->Kp / 2);
   k_tc_make_ay<<<(unsigned)((nay + 255) / 256), 256, 0, st>>>(U, a.W, C, M, p->S, p->Kp,
                                                               p->ay_hi, p->ay_lo);

@@ -32,8 +32,9 @@ cudaError_t coverage_db_run(const float *H, int S, int R, float threshold, float
                             float *out, cudaStream_t st);
 // Wait-timeout word: the kernels with bounded mbarrier waits set the word at
 // control-block offset 48 when a wait runs out; every call on such a path
-// clears it first (obj_begin_call), and the call's outputs are then NaN.
-cudaError_t obj_begin_call(unsigned *err, cudaStream_t st);
+// clears it first (its first kernel, or obj_begin_call), and the call's
+// outputs are then NaN.
+cudaError_t obj_begin_call(unsigned *err, bool cleared, cudaStream_t st);
 // test hook: the next `calls` calls on paths with bounded waits behave as if
 // one of their waits had run out
 void obj_inject_timeouts(int calls);

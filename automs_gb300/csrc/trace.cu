@@ -1331,12 +1331,14 @@ int stage2_per_sm() {
 }  // namespace
 
 int trace_paths_per_item(const TraceDev &P, unsigned long long n_tasks) {
-  // about 4 items per resident warp when every item takes one path; larger
-  // chunks (fewer atomic adds, longer items) only when the round is big
+  // several paths per item (fewer atomic adds) only when a round still has
+  // about 32 items per resident warp with them: long items at the end of a
+  // smaller round leave the GPU idle (coverage-128's first round: 9 paths
+  // per item, 1.94 ms, against about 1.6 ms one thread per ray)
   const unsigned long long warps = (unsigned long long)stage2_per_sm() * ams_device_sms() * 8;
   const unsigned long long pairs = (unsigned long long)(P.gs * P.gs) * P.n_src;
   const unsigned long long work = n_tasks * ((pairs + 31) / 32);
-  unsigned long long k = work / (4 * warps);
+  unsigned long long k = work / (32 * warps);
   if (k < 1) k = 1;
   if (k > 16) k = 16;
   return (int)k;
