@@ -208,6 +208,48 @@ def make_objective_fixtures():
             print(name, "loss", loss.item(), "dropped rows", int(drop.sum()))
 
 
+def make_postprocess_fixtures():
+    """go.Model.postprocess (go.py:89-97) on every objective case: the code
+    phases rounded to pi/2 steps, the metasurface phases reduced modulo
+    max_phase, then forward (go.py:159-245): the quantised parameters,
+    Model.result, Model.max_code_ids and the loss, with the dropout draw."""
+    import torch
+    with reference_go_on_cpu() as (go, saved):
+        for name in cases.OBJECTIVE_CASES:
+            c = cases.objective_case(name)
+            chans = {k: torch.from_numpy(v) for k, v in c["channels"].items()}
+            ms_list = [go.Metasurface(None, None, None, None, None, c["max_phase_deg"])
+                       for _ in range(c["n_ms"])]
+            model = go.Model(name, channels=chans, ms_list=ms_list,
+                             max_ms_reflex=c["max_ms_reflex"], code_num=c["code_num"], w=c["w"])
+            with torch.no_grad():
+                model.antenna_theta.copy_(torch.from_numpy(c["theta"]))
+                for i in range(c["n_ms"]):
+                    model.ms_theta[i].copy_(torch.from_numpy(c["phi"][i]) * 3.0)
+            box = {}
+            real_rand = torch.rand
+
+            def rand_hook(*a, **kw):
+                out = real_rand(*a, **kw)
+                box["r"] = out.clone()
+                return out
+            torch.manual_seed(c["seed"] + 50)
+            torch.rand = rand_hook
+            try:
+                model.postprocess()
+            finally:
+                torch.rand = real_rand
+            out = dict(theta_post=model.antenna_theta.detach().numpy(), rand=box["r"].numpy(),
+                       result=model.result.numpy(), max_code_ids=model.max_code_ids.numpy(),
+                       loss=np.float64(model.loss.item() if hasattr(model, "loss")
+                                       else model.forward().item()))
+            for i in range(c["n_ms"]):
+                out[f"phi_in{i}"] = (torch.from_numpy(c["phi"][i]) * 3.0).numpy()
+                out[f"phi_post{i}"] = model.ms_theta[i].detach().numpy()
+            np.savez_compressed(os.path.join(HERE, f"post_{name}.npz"), **out)
+            print("postprocess", name, "loss", float(out["loss"]))
+
+
 # ------------------------------------------------------------- geometry
 def geometry_inputs():
     """Seeded inputs of the geometry helpers (go.py:248-512, 1309-1338)."""
@@ -400,6 +442,9 @@ if __name__ == "__main__":
     if not REF or not oracle.ref_available():
         raise SystemExit("AMS_REFERENCE_ROOT does not name the reference tree; "
                          "fixtures cannot be regenerated")
+    if sys.argv[1:] == ["postprocess"]:
+        make_postprocess_fixtures()
+        raise SystemExit(0)
     if sys.argv[1:] == ["ref_scene"]:
         make_reference_scene_fixtures()
         raise SystemExit(0)
@@ -409,5 +454,6 @@ if __name__ == "__main__":
     make_unit_fixtures()
     make_channel_fixtures()
     make_objective_fixtures()
+    make_postprocess_fixtures()
     make_geometry_fixtures()
     make_reference_scene_fixtures()

@@ -360,3 +360,42 @@ def test_wait_timeout_is_reported(obj, path):
     assert torch.equal(again[1], clean[1]) and torch.equal(again[2], clean[2])
     if plan is not None:
         plan.close()
+
+
+@pytest.mark.parametrize("name", cases.OBJECTIVE_CASES)
+def test_postprocess_matches_reference_model(obj, name, monkeypatch):
+    """Model.postprocess (go.py:89-97) against go.Model's: code phases rounded
+    to pi/2 steps, metasurface phases reduced modulo max_phase, then the
+    forward pass: Model.result (|Y|), Model.max_code_ids and the loss, with
+    the reference's dropout draw replayed."""
+    from automs_gb300.geometry import Metasurface
+    g = np.load(os.path.join(GOLD, f"post_{name}.npz"))
+    c = cases.objective_case(name)
+    chans = {k: cuda(v) for k, v in c["channels"].items()}
+    ms = [Metasurface(None, None, None, None, None, c["max_phase_deg"]) for _ in range(c["n_ms"])]
+    m = obj.Model(name, chans, ms, max_ms_reflex=c["max_ms_reflex"], code_num=c["code_num"],
+                  w=c["w"], drop_rate=0.0)
+    with torch.no_grad():
+        m.antenna_theta.copy_(cuda(c["theta"]))
+        for i in range(c["n_ms"]):
+            m.ms_theta[i].copy_(cuda(g[f"phi_in{i}"]))
+    m.drop_rate = 0.1
+    drawn = torch.from_numpy(g["rand"])
+    monkeypatch.setattr(torch, "rand", lambda *a, **k: drawn.clone())
+    m.postprocess()
+    monkeypatch.undo()
+    np.testing.assert_array_equal(m.antenna_theta.detach().cpu().numpy(), g["theta_post"])
+    for i in range(c["n_ms"]):
+        np.testing.assert_allclose(m.ms_theta[i].detach().cpu().numpy(), g[f"phi_post{i}"],
+                                   rtol=0, atol=2e-6)
+        assert float(m.ms_theta[i].max()) < ms[i].max_phase
+    res = m.result.cpu().numpy()
+    np.testing.assert_allclose(res, g["result"], rtol=1e-4, atol=1e-4 * np.abs(g["result"]).max())
+    # the strongest code per Rx, wherever it leads the runner-up clearly
+    top2 = np.sort(g["result"], axis=0)[-2:] if g["result"].shape[0] > 1 else None
+    ids = m.max_code_ids.cpu().numpy()
+    clear = (np.ones(ids.shape, bool) if top2 is None
+             else (top2[1] - top2[0]) > 1e-3 * np.abs(g["result"]).max())
+    assert clear.mean() > 0.9
+    np.testing.assert_array_equal(ids[clear], g["max_code_ids"][clear])
+    np.testing.assert_allclose(float(m.loss), float(g["loss"]), rtol=2e-4)
