@@ -168,20 +168,183 @@ class PlacementStudy:
         return np.stack(X), np.stack(Y), P
 
 
+class TwoRoomStudy:
+    """Metasurface placement in a non-line-of-sight room: a pool of seeded
+    two-room floors (scenes.tworoom_scene); the AP (16-element ULA, 2.5 m,
+    facing +x) stands in room A 1.5 m before the door gap, the Rx grid covers
+    room B at 1.5 m, and the metasurface hangs on one of room B's three
+    walls facing into it.  Most of room B sees the AP only through the door,
+    so a well-placed metasurface adds several dB where the direct paths are
+    weak, the situation of the reference's trial (a metasurface lighting the
+    area a wall-mounted AP covers poorly, physical_exp_nni_model.py:26-87).
+
+    A placement is p = (scene, wall, u, v, n): the scene of the pool, the
+    wall (0: far wall x = a + b, 1: side y = 0, 2: side y = d), the position
+    along it and the height as fractions, and the side in elements
+    (lambda/2 pitch).  Its descriptor is 8 placement numbers and the scene's
+    64-value code (8 x 8 cells over the floor: the share of each cell taken
+    by walls and boxes, door gap included), so the code varies per sample."""
+
+    def __init__(self, n_scenes=16, seed=0, rx=(64, 64), launch=250, max_reflection=2,
+                 opt_steps=12, sizes=(16, 48)):
+        self.lam = scenes.WAVE_LEN_60GHZ
+        self.rx = rx
+        self.pool = 1
+        self.launch = launch
+        self.L = max_reflection
+        self.opt_steps = opt_steps
+        self.sizes = sizes
+        wv = np.ones(16, np.complex64) / 4.0
+        self.W = torch.as_tensor(wv[None], device="cuda")
+        self.scenes = []
+        for k in range(n_scenes):
+            tris, mat, mp, g = scenes.tworoom_scene(seed * 1000 + k)
+            a, b, d = g["a"], g["b"], g["d"]
+            ap = (a - 1.5, g["y_door"], 2.5)
+            src = scenes.ula(ap, (0, 1, 0), 16, self.lam / 2)
+            dst = scenes.rx_grid(a + 0.25, a + b - 0.25, rx[0], 0.25, d - 0.25, rx[1], 1.5)
+            sc = tracer.Scene(tris, mat, mp)
+            entry = dict(tris=tris, mat=mat, mat_prop=mp, geo=g, src=src, dst=dst, scene=sc,
+                         code=self._code(g))
+            H0, _ = self._trace(sc, src, dst, 2, 0, (1, 0, 0), (0, 0, 0))
+            entry["db0"] = self._coverage(H0)
+            self.scenes.append(entry)
+
+    # ------------------------------------------------------------ helpers
+    @staticmethod
+    def _code(g):
+        a, b, d, yd = g["a"], g["b"], g["d"], g["y_door"]
+        X = a + b
+        occ = np.zeros((8, 8))
+        rects = [((lo[0], lo[1]), (hi[0], hi[1])) for lo, hi in g["boxes"]]
+        t = 0.15  # walls as strips
+        rects += [((0, 0), (X, t)), ((0, d - t), (X, d)), ((0, 0), (t, d)), ((X - t, 0), (X, d)),
+                  ((a - t / 2, 0), (a + t / 2, yd - 0.6)), ((a - t / 2, yd + 0.6), (a + t / 2, d))]
+        for i in range(8):
+            for j in range(8):
+                cx0, cx1, cy0, cy1 = i * X / 8, (i + 1) * X / 8, j * d / 8, (j + 1) * d / 8
+                area = 0.0
+                for (x0, y0), (x1, y1) in rects:
+                    area += (max(0.0, min(x1, cx1) - max(x0, cx0))
+                             * max(0.0, min(y1, cy1) - max(y0, cy0)))
+                occ[i, j] = min(1.0, 8.0 * area / ((X / 8) * (d / 8)))
+        return occ.reshape(-1).astype(np.float32)
+
+    def _trace(self, scene, src, dst, sbp, dbp, sdir, ddir):
+        p = tracer.make_params(self.launch, self.launch, self.lam, self.L, 100, sbp, dbp, 5,
+                               0.5e-5, 0.06, sdir, ddir)
+        res, st = scene.trace(src, dst, p)
+        return torch.complex(res[..., 0], res[..., 1]), st
+
+    def _coverage(self, H):
+        return (20 * torch.log10((self.W @ H).abs()[0] + 1e-12)).reshape(-1)
+
+    def ms_geometry(self, p):
+        k, wall, u, v, n = int(p[0]), int(p[1]), float(p[2]), float(p[3]), int(p[4])
+        g = self.scenes[k]["geo"]
+        a, b, d = g["a"], g["b"], g["d"]
+        if wall == 0:
+            center, nrm = np.array([a + b, d * (0.05 + 0.9 * u), 0.0]), np.array([-1.0, 0, 0])
+        elif wall == 1:
+            center, nrm = np.array([a + b * (0.05 + 0.9 * u), 0.0, 0.0]), np.array([0, 1.0, 0])
+        else:
+            center, nrm = np.array([a + b * (0.05 + 0.9 * u), d, 0.0]), np.array([0, -1.0, 0])
+        center[2] = 0.5 + 2.0 * v
+        pos, quad, kdir = scenes.metasurface(center, nrm, (0, 0, -1), n, self.lam / 2)
+        return pos, quad, kdir
+
+    def descriptor(self, p):
+        k, wall, u, v, n = int(p[0]), int(p[1]), float(p[2]), float(p[3]), int(p[4])
+        lo, hi = self.sizes
+        dsc = np.zeros(N_PARAMS, np.float32)
+        dsc[wall] = 1.0
+        dsc[3], dsc[4] = u, v
+        dsc[5] = (n - lo) / max(1, hi - lo)
+        dsc[6], dsc[7] = math.sin(math.pi * u), math.cos(math.pi * u)
+        return np.concatenate([dsc, self.scenes[k]["code"]])
+
+    def random_params(self, rng, scene=None):
+        lo, hi = self.sizes
+        k = int(rng.integers(0, len(self.scenes))) if scene is None else int(scene)
+        return (k, int(rng.integers(0, 3)), float(rng.uniform(0.05, 0.95)),
+                float(rng.uniform(0.05, 0.95)), int(rng.integers(lo // 8, hi // 8 + 1) * 8))
+
+    def neighbour(self, p, rng):
+        """Annealing move within p's scene: another wall with probability
+        0.1, (u, v) by N(0, 0.08) clipped to [0.05, 0.95], the side by +-8
+        with probability 0.2 within the sizes."""
+        k, w, u, v, n = p
+        if rng.random() < 0.1:
+            w = int(rng.integers(0, 3))
+        u = float(np.clip(u + rng.normal(0, 0.08), 0.05, 0.95))
+        v = float(np.clip(v + rng.normal(0, 0.08), 0.05, 0.95))
+        if rng.random() < 0.2:
+            lo, hi = self.sizes
+            n = int(np.clip(n + 8 * rng.choice([-1, 1]), lo, hi))
+        return (k, w, u, v, n)
+
+    # ---------------------------------------------------------- one trial
+    def evaluate(self, p, return_detail=False):
+        """Trace + optimise one placement; returns its gain map (dB over the
+        Rx grid, with the optimised metasurface minus without)."""
+        e = self.scenes[int(p[0])]
+        pos, quad, nrm = self.ms_geometry(p)
+        sc = tracer.Scene(*scenes.with_blackholes(e["tris"], e["mat"], e["mat_prop"], [quad]))
+        Hd, _ = self._trace(sc, e["src"], e["dst"], 2, 0, (1, 0, 0), (0, 0, 0))
+        sc.close()
+        Ha, _ = self._trace(e["scene"], e["src"], pos, 2, 1, (1, 0, 0), nrm)
+        Hr, _ = self._trace(e["scene"], pos, e["dst"], 1, 0, nrm, (0, 0, 0))
+        M = pos.shape[0] * pos.shape[1]
+        phi = torch.zeros(M, device="cuda", requires_grad=True)
+        opt = torch.optim.Adam([phi], lr=0.3)
+        R = Hd.shape[1]
+        for _ in range(self.opt_steps):
+            loss = objective.capacity_objective(self.W, Hd, Ha, Hr, phi, 2 * math.pi, 1.0 / R)
+            loss.backward()
+            opt.step()
+            opt.zero_grad()
+        with torch.no_grad():
+            _, recv = objective.capacity_objective(self.W, Hd, Ha, Hr, phi.detach(), 2 * math.pi,
+                                                   1.0 / R, return_recv=True)
+            gain = (20 * torch.log10(recv[0] + 1e-12)).reshape(-1) - e["db0"]
+        if return_detail:
+            return gain, dict(phi=phi.detach())
+        return gain
+
+    def dataset(self, n, seed=0, log=None, scene=None):
+        rng = np.random.Generator(np.random.PCG64(seed))
+        X, Y, P = [], [], []
+        for i in range(n):
+            p = self.random_params(rng, scene)
+            X.append(self.descriptor(p))
+            Y.append(self.evaluate(p).float().cpu().numpy())
+            P.append(p)
+            if log and (i + 1) % 200 == 0:
+                log(f"{i + 1}/{n} samples")
+        return np.stack(X), np.stack(Y), P
+
+    def close(self):
+        for e in self.scenes:
+            e["scene"].close()
+
+
 def score(gain):
     """Placement figure of merit: mean pooled coverage gain (dB)."""
     return gain.mean(-1)
 
 
-def anneal_candidates(study, n, rng, surrogate=None, t0=1.0, t1=0.02, device="cuda"):
+def anneal_candidates(study, n, rng, surrogate=None, t0=1.0, t1=0.02, device="cuda",
+                      start=None):
     """Simulated-annealing chain over placements (the NNI Anneal tuner's role,
-    physical_exp_nni_main.py:11-29).  Moves: another wall with probability
-    0.1, the position (u, v) by N(0, 0.08) clipped to [0.1, 0.9], the size by
-    +-8 with probability 0.2 within study.sizes.  With a surrogate (a callable
-    on descriptors placed on `device`), moves are accepted on its predicted
-    score by the Metropolis rule at a temperature falling geometrically from
-    t0 to t1; every visited placement is returned."""
-    cur = study.random_params(rng)
+    physical_exp_nni_main.py:11-29), from `start` or a random placement.
+    Moves: study.neighbour when the study has one, else another wall with
+    probability 0.1, the position (u, v) by N(0, 0.08) clipped to [0.1, 0.9],
+    the size by +-8 with probability 0.2 within study.sizes.  With a
+    surrogate (a callable on descriptors placed on `device`), moves are
+    accepted on its predicted score by the Metropolis rule at a temperature
+    falling geometrically from t0 to t1; every visited placement is
+    returned."""
+    cur = study.random_params(rng) if start is None else start
     visited = [cur]
     cur_s = None
     batch = 256
@@ -190,6 +353,9 @@ def anneal_candidates(study, n, rng, surrogate=None, t0=1.0, t1=0.02, device="cu
         # propose a batch of neighbours, score them together
         props = []
         for _ in range(batch):
+            if hasattr(study, "neighbour"):
+                props.append(study.neighbour(cur, rng))
+                continue
             w, u, v, s = cur
             if rng.random() < 0.1:
                 w = int(rng.integers(0, 3))
@@ -212,6 +378,28 @@ def anneal_candidates(study, n, rng, surrogate=None, t0=1.0, t1=0.02, device="cu
             if len(visited) >= n:
                 break
     return visited[:n]
+
+
+def anneal_traced(study, n, rng, start, t0=1.0, t1=0.02):
+    """The plain annealing loop: the same Metropolis chain with every move
+    judged by the tracer (study.evaluate), as the reference's tuner judges
+    each trial by running it.  Returns the visited placements, their traced
+    scores and the wall time."""
+    torch.cuda.synchronize()
+    t_start = time.perf_counter()
+    cur = start
+    cur_s = float(score(study.evaluate(cur)))
+    seen, scores = [cur], [cur_s]
+    while len(seen) < n:
+        q = study.neighbour(cur, rng)
+        s_ = float(score(study.evaluate(q)))
+        T = t0 * (t1 / t0) ** (len(seen) / n)
+        if s_ > cur_s or rng.random() < math.exp((s_ - cur_s) / T):
+            cur, cur_s = q, s_
+        seen.append(q)
+        scores.append(s_)
+    torch.cuda.synchronize()
+    return seen, np.asarray(scores), time.perf_counter() - t_start
 
 
 def screening_report(study, mlp, pool_params, pool_gain, top_frac=0.05, t_trial=None,

@@ -302,6 +302,58 @@ def multiroom_scene(target_tris=200_000, rooms=(3, 3), seed=0, height=3.0):
     return tris, mat, mat_prop, xs, ys
 
 
+def tworoom_scene(seed=0, height=3.0):
+    """Seeded two-room floor for the placement study: room A = [0, a] and
+    room B = [a, a + b] along x, both [0, d] along y, with a, b, d U[6, 10] m;
+    the wall between them has a 1.2 m wide, 2.1 m tall door gap centred at
+    y_door U[1.5, d - 1.5]; 4 to 10 floor-standing boxes per room (footprint
+    U[0.2, 1.5]^2, height U[0.3, 2.0], one quad per face), kept clear of the
+    door.  Materials as shoebox_scene.  Returns tris, mat, mat_prop and a
+    dict of the geometry (a, b, d, y_door, box bounds)."""
+    rng = np.random.Generator(np.random.PCG64(5000 + seed))
+    a, b, d = (float(x) for x in rng.uniform(6.0, 10.0, 3))
+    y_door = float(rng.uniform(1.5, d - 1.5))
+    X, Z = a + b, height
+    tris, mats = [], []
+    props = [rng.uniform(0.3, 0.7) for _ in range(3)]
+    ex, ey, ez = np.array([X, 0, 0.0]), np.array([0, d, 0.0]), np.array([0, 0, Z])
+    floor = _quad_grid(np.zeros(3), ex, ey, 2, 2)
+    ceil = _quad_grid(ez, ex, ey, 2, 2)
+    walls = (_quad_grid(np.zeros(3), ex, ez, 2, 1) + _quad_grid(ey, ex, ez, 2, 1)
+             + _quad_grid(np.zeros(3), ey, ez, 1, 1) + _quad_grid(ex, ey, ez, 1, 1))
+    # the wall between the rooms, with the door gap
+    y0, y1 = y_door - 0.6, y_door + 0.6
+    p = np.array([a, 0.0, 0.0])
+    walls += _quad_grid(p, np.array([0, y0, 0.0]), ez, 1, 1)
+    walls += _quad_grid(p + np.array([0, y1, 0.0]), np.array([0, d - y1, 0.0]), ez, 1, 1)
+    walls += _quad_grid(p + np.array([0, y0, 2.1]), np.array([0, y1 - y0, 0.0]),
+                        np.array([0, 0, Z - 2.1]), 1, 1)
+    for group, m in ((floor, 0), (ceil, 1), (walls, 2)):
+        tris += group
+        mats += [m] * len(group)
+    boxes = []
+    for x0, x1 in ((0.0, a), (a, X)):
+        for _ in range(int(rng.integers(4, 11))):
+            while True:
+                sx, sy = rng.uniform(0.2, 1.5, size=2)
+                h = rng.uniform(0.3, 2.0)
+                cx, cy = rng.uniform(x0 + 0.3, x1 - 0.3), rng.uniform(0.3, d - 0.3)
+                lo = np.array([max(cx - sx / 2, x0 + 0.05), max(cy - sy / 2, 0.05), 0.0])
+                hi = np.array([min(cx + sx / 2, x1 - 0.05), min(cy + sy / 2, d - 0.05), h])
+                near_door = (abs(cx - a) < 2.0 and abs(cy - y_door) < 2.0)
+                if not near_door:
+                    break
+            bt = box_tris(lo, hi, 1)
+            tris += bt
+            mats += [len(props)] * len(bt)
+            props.append(rng.uniform(0.3, 0.7))
+            boxes.append((lo, hi))
+    tris = np.asarray(tris, np.float32)
+    mat = np.asarray(mats, np.int32)
+    mat_prop = np.repeat(np.asarray(props, np.float32)[:, None], 19, axis=1)
+    return tris, mat, mat_prop, dict(a=a, b=b, d=d, y_door=y_door, boxes=boxes)
+
+
 def batch_config(n_place=64, seed=0, target_tris=200_000, n_rx=256, launch=1000):
     """Batched hyper-configs: a multi-room building (multiroom_scene), a
     16-element AP in the middle room at 2.5 m facing +y, an n_rx x n_rx Rx
