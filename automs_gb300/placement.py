@@ -236,8 +236,13 @@ class TwoRoomStudy:
         res, st = scene.trace(src, dst, p)
         return torch.complex(res[..., 0], res[..., 1]), st
 
+    # coverage floor (dB): an Rx without paths counts as this, so a gain is
+    # the rise above the floor, not above -240 dB
+    FLOOR_DB = -110.0
+
     def _coverage(self, H):
-        return (20 * torch.log10((self.W @ H).abs()[0] + 1e-12)).reshape(-1)
+        db = 20 * torch.log10((self.W @ H).abs()[0] + 1e-12)
+        return db.clamp_min(self.FLOOR_DB).reshape(-1)
 
     def ms_geometry(self, p):
         k, wall, u, v, n = int(p[0]), int(p[1]), float(p[2]), float(p[3]), int(p[4])
@@ -306,7 +311,8 @@ class TwoRoomStudy:
         with torch.no_grad():
             _, recv = objective.capacity_objective(self.W, Hd, Ha, Hr, phi.detach(), 2 * math.pi,
                                                    1.0 / R, return_recv=True)
-            gain = (20 * torch.log10(recv[0] + 1e-12)).reshape(-1) - e["db0"]
+            db = (20 * torch.log10(recv[0] + 1e-12)).clamp_min(self.FLOOR_DB).reshape(-1)
+            gain = db - e["db0"]
         if return_detail:
             return gain, dict(phi=phi.detach())
         return gain
