@@ -259,14 +259,25 @@ class TwoRoomStudy:
         return pos, quad, kdir
 
     def descriptor(self, p):
-        k, wall, u, v, n = int(p[0]), int(p[1]), float(p[2]), float(p[3]), int(p[4])
+        """8 placement numbers in the scene's frame -- the metasurface
+        centre's offset from the AP (x, y, z over 10 m), its normal (x, y),
+        its side (0..1 over the sizes), the cosine between its normal and
+        the direction to the door gap's centre and its distance to that
+        centre (over 10 m) -- then the scene's 64-value code."""
+        k, n = int(p[0]), int(p[4])
+        e = self.scenes[k]
+        g = e["geo"]
         lo, hi = self.sizes
-        dsc = np.zeros(N_PARAMS, np.float32)
-        dsc[wall] = 1.0
-        dsc[3], dsc[4] = u, v
-        dsc[5] = (n - lo) / max(1, hi - lo)
-        dsc[6], dsc[7] = math.sin(math.pi * u), math.cos(math.pi * u)
-        return np.concatenate([dsc, self.scenes[k]["code"]])
+        pos, _, nrm = self.ms_geometry(p)
+        c = pos.reshape(-1, 3).mean(0).astype(np.float64)
+        ap = e["src"].reshape(-1, 3).mean(0).astype(np.float64)
+        door = np.array([g["a"], g["y_door"], 1.05])
+        to_door = door - c
+        dist = float(np.linalg.norm(to_door))
+        dsc = np.array([(c[0] - ap[0]) / 10, (c[1] - ap[1]) / 10, (c[2] - ap[2]) / 10,
+                        float(nrm[0]), float(nrm[1]), (n - lo) / max(1, hi - lo),
+                        float(np.dot(nrm, to_door)) / max(dist, 1e-6), dist / 10], np.float32)
+        return np.concatenate([dsc, e["code"]])
 
     def random_params(self, rng, scene=None):
         lo, hi = self.sizes

@@ -480,6 +480,14 @@ def surrogate_bench(torch, n_train=1000, n_val=200, n_cand=5000, top_frac=0.05, 
     pva = predict(torch.as_tensor(Xva).cuda()).cpu().numpy()
     err_net = float(np.median(np.abs(pva - Yva)))
     err_mean = float(np.median(np.abs(mu[None] - Yva)))
+    lit = np.abs(Yva) >= 1.0  # cells the metasurface moves by a dB or more
+    err_lit = float(np.median(np.abs(pva - Yva)[lit])) if lit.any() else None
+    err_lit_mean = float(np.median(np.abs(mu[None] - Yva)[lit])) if lit.any() else None
+    s_true, s_pred = Yva.mean(1), pva.mean(1)
+    err_score = float(np.median(np.abs(s_pred - s_true)))
+    err_score_mean = float(np.median(np.abs(mu.mean() - s_true)))
+    rank_corr = float(np.corrcoef(np.argsort(np.argsort(s_pred)),
+                                  np.argsort(np.argsort(s_true)))[0, 1])
     rows = []
     for k in test_scenes:
         rng = np.random.Generator(np.random.PCG64(100 + k))
@@ -513,6 +521,10 @@ def surrogate_bench(torch, n_train=1000, n_val=200, n_cand=5000, top_frac=0.05, 
             "mean_predictor_median_abs_err_db": err_mean,
             "err_ratio_vs_mean_predictor": err_net / err_mean,
             "median_abs_gain_db": float(np.median(np.abs(Yva))),
+            "cells_gain_ge_1db": float(lit.mean()),
+            "median_abs_err_db_cells_ge_1db": [err_lit, err_lit_mean],
+            "score_median_abs_err_db": [err_score, err_score_mean],
+            "score_rank_correlation": rank_corr,
             "best_gain_db_screened_vs_plain": [[r["screened_best_db"], r["plain_best_db"]]
                                                for r in rows],
             "config": {"workload": "two-room NLOS study: 16 floors, 64x64 Rx in room B, "
