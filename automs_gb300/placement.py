@@ -261,9 +261,11 @@ class TwoRoomStudy:
     def descriptor(self, p):
         """8 placement numbers in the scene's frame -- the metasurface
         centre's offset from the AP (x, y, z over 10 m), its normal (x, y),
-        its side (0..1 over the sizes), the cosine between its normal and
-        the direction to the door gap's centre and its distance to that
-        centre (over 10 m) -- then the scene's 64-value code."""
+        its side (0..1 over the sizes), and where the line from the AP to
+        that centre crosses the wall between the rooms: its offset from the
+        door gap's centre over the gap's half width, and its height over
+        the gap's height (both within 1: the AP sees the metasurface through
+        the door) -- then the scene's 64-value code."""
         k, n = int(p[0]), int(p[4])
         e = self.scenes[k]
         g = e["geo"]
@@ -271,12 +273,12 @@ class TwoRoomStudy:
         pos, _, nrm = self.ms_geometry(p)
         c = pos.reshape(-1, 3).mean(0).astype(np.float64)
         ap = e["src"].reshape(-1, 3).mean(0).astype(np.float64)
-        door = np.array([g["a"], g["y_door"], 1.05])
-        to_door = door - c
-        dist = float(np.linalg.norm(to_door))
+        t = (g["a"] - ap[0]) / (c[0] - ap[0])  # the metasurface lies beyond the wall
+        y_at = ap[1] + t * (c[1] - ap[1])
+        z_at = ap[2] + t * (c[2] - ap[2])
         dsc = np.array([(c[0] - ap[0]) / 10, (c[1] - ap[1]) / 10, (c[2] - ap[2]) / 10,
                         float(nrm[0]), float(nrm[1]), (n - lo) / max(1, hi - lo),
-                        float(np.dot(nrm, to_door)) / max(dist, 1e-6), dist / 10], np.float32)
+                        (y_at - g["y_door"]) / 0.6, z_at / 2.1], np.float32)
         return np.concatenate([dsc, e["code"]])
 
     def random_params(self, rng, scene=None):

@@ -445,7 +445,7 @@ def objective_codes_bench(torch, R=4096, C=60, nset=4, reps=20):
                                 "mma_flop_per_eval": mma_flop, "peak_kind": "measured bf16 burst"}}
 
 
-def surrogate_bench(torch, n_train=1000, n_val=200, n_cand=5000, top_frac=0.05, n_scenes=16,
+def surrogate_bench(torch, n_train=1500, n_val=200, n_cand=5000, top_frac=0.05, n_scenes=16,
                     test_scenes=(3, 11)):
     """Surrogate-screened placement search against the plain tracer-judged
     annealing loop (placement.TwoRoomStudy: 16 seeded two-room floors, AP in
