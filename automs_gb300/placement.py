@@ -265,7 +265,8 @@ class TwoRoomStudy:
         that centre crosses the wall between the rooms: its offset from the
         door gap's centre over the gap's half width, and its height over
         the gap's height (both within 1: the AP sees the metasurface through
-        the door) -- then the scene's 64-value code."""
+        the door; both clipped to [-3, 3]) -- then the scene's 64-value
+        code."""
         k, n = int(p[0]), int(p[4])
         e = self.scenes[k]
         g = e["geo"]
@@ -278,7 +279,8 @@ class TwoRoomStudy:
         z_at = ap[2] + t * (c[2] - ap[2])
         dsc = np.array([(c[0] - ap[0]) / 10, (c[1] - ap[1]) / 10, (c[2] - ap[2]) / 10,
                         float(nrm[0]), float(nrm[1]), (n - lo) / max(1, hi - lo),
-                        (y_at - g["y_door"]) / 0.6, z_at / 2.1], np.float32)
+                        float(np.clip((y_at - g["y_door"]) / 0.6, -3, 3)),
+                        float(np.clip(z_at / 2.1, -3, 3))], np.float32)
         return np.concatenate([dsc, e["code"]])
 
     def random_params(self, rng, scene=None):

@@ -470,7 +470,7 @@ def surrogate_bench(torch, n_train=1500, n_val=200, n_cand=5000, top_frac=0.05, 
     net = surrogate.MLP([Xtr.shape[1], 512, 512, 512, 512, Ytr.shape[1]], max_batch=4096, seed=0)
     t0 = time.perf_counter()
     hist = net.fit(torch.as_tensor(Xtr).cuda(), torch.as_tensor((Ytr - mu) / sd).cuda(),
-                   epochs=200, batch=64, lr=1e-3, lr_decay=0.985)
+                   epochs=400, batch=64, lr=1e-3, lr_decay=0.995)
     torch.cuda.synchronize()
     t_fit = time.perf_counter() - t0
     mu_t = torch.as_tensor(mu, device="cuda")
@@ -522,6 +522,7 @@ def surrogate_bench(torch, n_train=1500, n_val=200, n_cand=5000, top_frac=0.05, 
             "err_ratio_vs_mean_predictor": err_net / err_mean,
             "median_abs_gain_db": float(np.median(np.abs(Yva))),
             "cells_gain_ge_1db": float(lit.mean()),
+            "placements_score_ge_0p5db": float((s_true >= 0.5).mean()),
             "median_abs_err_db_cells_ge_1db": [err_lit, err_lit_mean],
             "score_median_abs_err_db": [err_score, err_score_mean],
             "score_rank_correlation": rank_corr,
