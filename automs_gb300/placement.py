@@ -171,7 +171,7 @@ class PlacementStudy:
 class TwoRoomStudy:
     """Metasurface placement in a non-line-of-sight room: a pool of seeded
     two-room floors (scenes.tworoom_scene); the AP (16-element ULA, 2.5 m,
-    facing +x) stands in room A 1.5 m before the door gap, the Rx grid covers
+    facing +x) stands in room A 0.5 m before the door gap, the Rx grid covers
     room B at 1.5 m, and the metasurface hangs on one of room B's three
     walls facing into it.  Most of room B sees the AP only through the door,
     so a well-placed metasurface adds several dB where the direct paths are
@@ -200,7 +200,7 @@ class TwoRoomStudy:
         for k in range(n_scenes):
             tris, mat, mp, g = scenes.tworoom_scene(seed * 1000 + k)
             a, b, d = g["a"], g["b"], g["d"]
-            ap = (a - 1.5, g["y_door"], 2.5)
+            ap = (a - 0.5, g["y_door"], 2.5)
             src = scenes.ula(ap, (0, 1, 0), 16, self.lam / 2)
             dst = scenes.rx_grid(a + 0.25, a + b - 0.25, rx[0], 0.25, d - 0.25, rx[1], 1.5)
             sc = tracer.Scene(tris, mat, mp)
@@ -219,7 +219,8 @@ class TwoRoomStudy:
         rects = [((lo[0], lo[1]), (hi[0], hi[1])) for lo, hi in g["boxes"]]
         t = 0.15  # walls as strips
         rects += [((0, 0), (X, t)), ((0, d - t), (X, d)), ((0, 0), (t, d)), ((X - t, 0), (X, d)),
-                  ((a - t / 2, 0), (a + t / 2, yd - 0.6)), ((a - t / 2, yd + 0.6), (a + t / 2, d))]
+                  ((a - t / 2, 0), (a + t / 2, yd - g["door_half"])),
+                  ((a - t / 2, yd + g["door_half"]), (a + t / 2, d))]
         for i in range(8):
             for j in range(8):
                 cx0, cx1, cy0, cy1 = i * X / 8, (i + 1) * X / 8, j * d / 8, (j + 1) * d / 8
@@ -279,7 +280,7 @@ class TwoRoomStudy:
         z_at = ap[2] + t * (c[2] - ap[2])
         dsc = np.array([(c[0] - ap[0]) / 10, (c[1] - ap[1]) / 10, (c[2] - ap[2]) / 10,
                         float(nrm[0]), float(nrm[1]), (n - lo) / max(1, hi - lo),
-                        float(np.clip((y_at - g["y_door"]) / 0.6, -3, 3)),
+                        float(np.clip((y_at - g["y_door"]) / g["door_half"], -3, 3)),
                         float(np.clip(z_at / 2.1, -3, 3))], np.float32)
         return np.concatenate([dsc, e["code"]])
 
