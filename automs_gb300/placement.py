@@ -169,19 +169,20 @@ class PlacementStudy:
 
 
 class TwoRoomStudy:
-    """Metasurface placement in a non-line-of-sight room: a pool of seeded
+    """Metasurface placement for a non-line-of-sight room: a pool of seeded
     two-room floors (scenes.tworoom_scene); the AP (16-element ULA, 2.5 m,
-    facing +x) stands in room A 0.5 m before the door gap, the Rx grid covers
-    room B at 1.5 m, and the metasurface hangs on one of room B's three
-    walls facing into it.  Most of room B sees the AP only through the door,
-    so a well-placed metasurface adds several dB where the direct paths are
-    weak, the situation of the reference's trial (a metasurface lighting the
-    area a wall-mounted AP covers poorly, physical_exp_nni_model.py:26-87).
+    facing +x) stands in room A 1.5 m before the door gap, the Rx grid covers
+    room B at 1.5 m, and the metasurface hangs on one of room A's three
+    other walls, facing into room A, where the AP lights it.  Most of room B
+    sees the AP only through the door at a narrow angle; a metasurface that
+    also sees through the door relays power into the rest of it, the
+    situation of the reference's trial (a metasurface lighting the area a
+    wall-mounted AP covers poorly, physical_exp_nni_model.py:26-87).
 
     A placement is p = (scene, wall, u, v, n): the scene of the pool, the
-    wall (0: far wall x = a + b, 1: side y = 0, 2: side y = d), the position
-    along it and the height as fractions, and the side in elements
-    (lambda/2 pitch).  Its descriptor is 8 placement numbers and the scene's
+    wall (0: back wall x = 0, 1: side y = 0, 2: side y = d, both over room
+    A), the position along it and the height as fractions, and the side in
+    elements (lambda/2 pitch).  Its descriptor is 8 placement numbers and the scene's
     64-value code (8 x 8 cells over the floor: the share of each cell taken
     by walls and boxes, door gap included), so the code varies per sample."""
 
@@ -200,7 +201,7 @@ class TwoRoomStudy:
         for k in range(n_scenes):
             tris, mat, mp, g = scenes.tworoom_scene(seed * 1000 + k)
             a, b, d = g["a"], g["b"], g["d"]
-            ap = (a - 0.5, g["y_door"], 2.5)
+            ap = (a - 1.5, g["y_door"], 2.5)
             src = scenes.ula(ap, (0, 1, 0), 16, self.lam / 2)
             dst = scenes.rx_grid(a + 0.25, a + b - 0.25, rx[0], 0.25, d - 0.25, rx[1], 1.5)
             sc = tracer.Scene(tris, mat, mp)
@@ -250,11 +251,11 @@ class TwoRoomStudy:
         g = self.scenes[k]["geo"]
         a, b, d = g["a"], g["b"], g["d"]
         if wall == 0:
-            center, nrm = np.array([a + b, d * (0.05 + 0.9 * u), 0.0]), np.array([-1.0, 0, 0])
+            center, nrm = np.array([0.0, d * (0.05 + 0.9 * u), 0.0]), np.array([1.0, 0, 0])
         elif wall == 1:
-            center, nrm = np.array([a + b * (0.05 + 0.9 * u), 0.0, 0.0]), np.array([0, 1.0, 0])
+            center, nrm = np.array([a * (0.05 + 0.9 * u), 0.0, 0.0]), np.array([0, 1.0, 0])
         else:
-            center, nrm = np.array([a + b * (0.05 + 0.9 * u), d, 0.0]), np.array([0, -1.0, 0])
+            center, nrm = np.array([a * (0.05 + 0.9 * u), d, 0.0]), np.array([0, -1.0, 0])
         center[2] = 0.5 + 2.0 * v
         pos, quad, kdir = scenes.metasurface(center, nrm, (0, 0, -1), n, self.lam / 2)
         return pos, quad, kdir
@@ -262,12 +263,12 @@ class TwoRoomStudy:
     def descriptor(self, p):
         """8 placement numbers in the scene's frame -- the metasurface
         centre's offset from the AP (x, y, z over 10 m), its normal (x, y),
-        its side (0..1 over the sizes), and where the line from the AP to
-        that centre crosses the wall between the rooms: its offset from the
-        door gap's centre over the gap's half width, and its height over
-        the gap's height (both within 1: the AP sees the metasurface through
-        the door; both clipped to [-3, 3]) -- then the scene's 64-value
-        code."""
+        its side (0..1 over the sizes), and where the line from that centre
+        to the centre of room B crosses the wall between the rooms: its
+        offset from the door gap's centre over the gap's half width, and its
+        height over the gap's height (both within 1: the metasurface looks
+        into room B through the door; both clipped to [-3, 3]) -- then the
+        scene's 64-value code."""
         k, n = int(p[0]), int(p[4])
         e = self.scenes[k]
         g = e["geo"]
@@ -275,9 +276,10 @@ class TwoRoomStudy:
         pos, _, nrm = self.ms_geometry(p)
         c = pos.reshape(-1, 3).mean(0).astype(np.float64)
         ap = e["src"].reshape(-1, 3).mean(0).astype(np.float64)
-        t = (g["a"] - ap[0]) / (c[0] - ap[0])  # the metasurface lies beyond the wall
-        y_at = ap[1] + t * (c[1] - ap[1])
-        z_at = ap[2] + t * (c[2] - ap[2])
+        rb = np.array([g["a"] + g["b"] / 2, g["d"] / 2, 1.5])
+        t = (g["a"] - c[0]) / (rb[0] - c[0])  # room B's centre lies beyond the wall
+        y_at = c[1] + t * (rb[1] - c[1])
+        z_at = c[2] + t * (rb[2] - c[2])
         dsc = np.array([(c[0] - ap[0]) / 10, (c[1] - ap[1]) / 10, (c[2] - ap[2]) / 10,
                         float(nrm[0]), float(nrm[1]), (n - lo) / max(1, hi - lo),
                         float(np.clip((y_at - g["y_door"]) / g["door_half"], -3, 3)),

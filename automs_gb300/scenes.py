@@ -305,7 +305,7 @@ def multiroom_scene(target_tris=200_000, rooms=(3, 3), seed=0, height=3.0):
 def tworoom_scene(seed=0, height=3.0):
     """Seeded two-room floor for the placement study: room A = [0, a] and
     room B = [a, a + b] along x, both [0, d] along y, with a, b, d U[6, 10] m;
-    the wall between them has a 2 m wide, 2.1 m tall door gap centred at
+    the wall between them has a 1.2 m wide, 2.1 m tall door gap centred at
     y_door U[1.5, d - 1.5]; 4 to 10 floor-standing boxes per room (footprint
     U[0.2, 1.5]^2, height U[0.3, 2.0], one quad per face), kept clear of the
     door.  Materials as shoebox_scene.  Returns tris, mat, mat_prop and a
@@ -322,7 +322,7 @@ def tworoom_scene(seed=0, height=3.0):
     walls = (_quad_grid(np.zeros(3), ex, ez, 2, 1) + _quad_grid(ey, ex, ez, 2, 1)
              + _quad_grid(np.zeros(3), ey, ez, 1, 1) + _quad_grid(ex, ey, ez, 1, 1))
     # the wall between the rooms, with the door gap
-    y0, y1 = y_door - 1.0, y_door + 1.0
+    y0, y1 = y_door - 0.6, y_door + 0.6
     p = np.array([a, 0.0, 0.0])
     walls += _quad_grid(p, np.array([0, y0, 0.0]), ez, 1, 1)
     walls += _quad_grid(p + np.array([0, y1, 0.0]), np.array([0, d - y1, 0.0]), ez, 1, 1)
@@ -351,7 +351,7 @@ def tworoom_scene(seed=0, height=3.0):
     tris = np.asarray(tris, np.float32)
     mat = np.asarray(mats, np.int32)
     mat_prop = np.repeat(np.asarray(props, np.float32)[:, None], 19, axis=1)
-    return tris, mat, mat_prop, dict(a=a, b=b, d=d, y_door=y_door, door_half=1.0, boxes=boxes)
+    return tris, mat, mat_prop, dict(a=a, b=b, d=d, y_door=y_door, door_half=0.6, boxes=boxes)
 
 
 def batch_config(n_place=64, seed=0, target_tris=200_000, n_rx=256, launch=1000):
