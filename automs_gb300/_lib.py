@@ -76,6 +76,9 @@ SIGNATURES = {
     "ams_objective_plan_bytes": (C.c_ulonglong, [_P]),
     "ams_objective_plan_destroy": (None, [_P]),
     "ams_objective_status": (_I, [_P, _P, _E, _S]),
+    "ams_objective_plan_create_stacked": (_I, [_P, _P, _I, _I, _I, _I, _P, C.POINTER(_P), _E, _S]),
+    "ams_objective_plan_coef_fwd_bwd": (_I, [_P, _P, _P, _I, _F, _P, _P, _P, _P, _P, _P, _E, _S]),
+    "ams_cgemm": (_I, [_I, _I, _I, _P, _I, _I, _P, _I, _I, _P, _I, _I, _P, _E, _S]),
     "ams_debug_inject_wait_timeout": (None, [_I]),
     "ams_coverage_db": (_I, [_P, _I, _I, _F, _F, _P, _P, _E, _S]),
     "ams_scratch_bytes": (C.c_ulonglong, []),

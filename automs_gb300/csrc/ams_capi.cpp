@@ -751,6 +751,7 @@ ams_status ams_objective_fwd_bwd_noalloc(const float *H_d, const float *H_a, con
 struct ams_objective_plan {
   ObjTcPlan *p;
   int S, M, R, Cmax;
+  bool stacked = false;  // made by ams_objective_plan_create_stacked (no H_a)
 };
 
 ams_status ams_objective_plan_create(const float *H_d, const float *H_a, const float *H_r, int S,
@@ -775,7 +776,7 @@ ams_status ams_objective_plan_create(const float *H_d, const float *H_a, const f
   }
   ObjTcPlan *tp = nullptr;
   CK(obj_tc_plan_create(H_d, H_a, H_r, S, M, R, C_max, (cudaStream_t)stream, &tp));
-  *out = new ams_objective_plan{tp, S, M, R, C_max};
+  *out = new ams_objective_plan{tp, S, M, R, C_max, false};
   return AMS_OK;
 }
 
@@ -792,6 +793,10 @@ ams_status ams_objective_plan_fwd_bwd(ams_objective_plan *plan, const float *phi
     return AMS_ERR_ARG;
   }
   if (!(max_phase > 0.f)) { set_err(errbuf, errlen, "max_phase must be > 0"); return AMS_ERR_ARG; }
+  if (plan->stacked) {
+    set_err(errbuf, errlen, "a stacked plan takes its coefficients: ams_objective_plan_coef_fwd_bwd");
+    return AMS_ERR_ARG;
+  }
   if (grad_Y && obj_tc_plan_streams(plan->p)) {
     set_err(errbuf, errlen, "grad_Y is not available from a plan made with C_max <= 2");
     return AMS_ERR_ARG;
@@ -799,6 +804,71 @@ ams_status ams_objective_plan_fwd_bwd(ams_objective_plan *plan, const float *phi
   ObjArgs a{nullptr, nullptr, nullptr, phi, W, max_phase, plan->S, plan->M, plan->R, C, w, drop,
             loss, grad_W, grad_phi, recv_amp, grad_Y};
   CK(obj_tc_run(plan->p, a, (cudaStream_t)stream));
+  return AMS_OK;
+}
+
+ams_status ams_objective_plan_create_stacked(const float *H_d, const float *H_r, int S, int M,
+                                             int R, int C_max, void *stream,
+                                             ams_objective_plan **out, char *errbuf,
+                                             size_t errlen) {
+  clear_stale_error();
+  if (!out) { set_err(errbuf, errlen, "out is NULL"); return AMS_ERR_ARG; }
+  *out = nullptr;
+  if (!H_d || !H_r) { set_err(errbuf, errlen, "a stacked plan needs H_d and H_r"); return AMS_ERR_ARG; }
+  if (S <= 0 || M <= 0 || R <= 0 || C_max <= 0 || C_max > 64) {
+    set_err(errbuf, errlen, "need S, M, R > 0 and 1 <= C_max <= 64 (S=%d M=%d R=%d C_max=%d)", S,
+            M, R, C_max);
+    return AMS_ERR_ARG;
+  }
+  if ((reinterpret_cast<uintptr_t>(H_d) | reinterpret_cast<uintptr_t>(H_r)) & 7) {
+    set_err(errbuf, errlen, "complex arrays must be 8-byte aligned");
+    return AMS_ERR_ARG;
+  }
+  ObjTcPlan *tp = nullptr;
+  CK(obj_tc_plan_create(H_d, nullptr, H_r, S, M, R, C_max, (cudaStream_t)stream, &tp, true));
+  *out = new ams_objective_plan{tp, S, M, R, C_max, true};
+  return AMS_OK;
+}
+
+ams_status ams_objective_plan_coef_fwd_bwd(ams_objective_plan *plan, const float *U,
+                                           const float *W, int C, float w, const uint8_t *drop,
+                                           float *loss, float *grad_U, float *grad_W,
+                                           float *recv_amp, void *stream, char *errbuf,
+                                           size_t errlen) {
+  clear_stale_error();
+  if (!plan || !plan->p) { set_err(errbuf, errlen, "plan is NULL"); return AMS_ERR_ARG; }
+  if (!plan->stacked) {
+    set_err(errbuf, errlen, "coefficients are taken by plans from ams_objective_plan_create_stacked");
+    return AMS_ERR_ARG;
+  }
+  if (!U || !W || !loss) { set_err(errbuf, errlen, "U, W and loss are required"); return AMS_ERR_ARG; }
+  if (C <= 0 || C > plan->Cmax) {
+    set_err(errbuf, errlen, "C=%d outside [1, %d] of this plan", C, plan->Cmax);
+    return AMS_ERR_ARG;
+  }
+  ObjArgs a{nullptr, nullptr, nullptr, nullptr, W, 1.0f, plan->S, plan->M, plan->R, C, w, drop,
+            loss, grad_W, nullptr, recv_amp, nullptr};
+  a.U_in = U;
+  a.grad_U = grad_U;
+  CK(obj_tc_run(plan->p, a, (cudaStream_t)stream));
+  return AMS_OK;
+}
+
+ams_status ams_cgemm(int m, int n, int k, const float *A, int lda, int opA, const float *B,
+                     int ldb, int opB, float *Cm, int ldc, int accumulate, void *stream,
+                     char *errbuf, size_t errlen) {
+  clear_stale_error();
+  if (!A || !B || !Cm || m <= 0 || n <= 0 || k <= 0 || opA < 0 || opA > 3 || opB < 0 ||
+      opB > 3) {
+    set_err(errbuf, errlen, "bad complex GEMM arguments (m=%d n=%d k=%d opA=%d opB=%d)", m, n, k,
+            opA, opB);
+    return AMS_ERR_ARG;
+  }
+  if (lda < (opA == 0 || opA == 3 ? k : m) || ldb < (opB == 0 || opB == 3 ? n : k) || ldc < n) {
+    set_err(errbuf, errlen, "leading dimensions too small");
+    return AMS_ERR_ARG;
+  }
+  CK(cgemm_run(m, n, k, A, lda, opA, B, ldb, opB, Cm, ldc, accumulate != 0, (cudaStream_t)stream));
   return AMS_OK;
 }
 

@@ -812,6 +812,17 @@ __global__ void __launch_bounds__(128) k_tc_dw_part(const float *GU, const float
   }
 }
 
+// out[c][j] = GU[c][k0 + j], j < n (complex), NaN after a run-out wait
+__global__ void k_tc_copy_rows(const float *GU, int K, int k0, int n, int C, float *out,
+                               const unsigned *err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= C * n) return;
+  const int c = i / n, j = i % n;
+  float2 v = __ldg(reinterpret_cast<const float2 *>(GU) + (size_t)c * K + k0 + j);
+  if (obj_failed(err)) v = make_float2(obj_nan(), obj_nan());
+  reinterpret_cast<float2 *>(out)[i] = v;
+}
+
 __global__ void k_tc_dw_sum(const float *GU, const float *dwp, int C, int S, int M, int K,
                             float *grad_W, const unsigned *err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2075,7 +2086,8 @@ cudaError_t run_plan_stream(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st) {
 }  // namespace
 
 cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr, int S, int M,
-                               int R, int Cmax, cudaStream_t st, ObjTcPlan **out) {
+                               int R, int Cmax, cudaStream_t st, ObjTcPlan **out,
+                               bool force_tc) {
   *out = nullptr;
   if (S <= 0 || M <= 0 || R <= 0 || Cmax <= 0 || Cmax > 64) return cudaErrorInvalidValue;
   ObjTcPlan *p = new ObjTcPlan();
@@ -2091,7 +2103,7 @@ cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr
   // stream mode when the streaming kernel's per-thread rows cover K (16 rows
   // a thread for one code, 8 for two); otherwise the tensor-core mode
   const int kpt = (p->K + 255) / 256;
-  if (Cmax <= 2 && kpt <= (Cmax == 1 ? 16 : 8)) return plan_stream_create(p, st, out);
+  if (!force_tc && Cmax <= 2 && kpt <= (Cmax == 1 ? 16 : 8)) return plan_stream_create(p, st, out);
   pick_split((p->Rp / tcg::BN) * (p->Mp / tcg::BM), p->Kp / tcg::BK, sms, p->ksy, p->kpy);
   pick_split((p->Np / tcg::BN) * (p->Mp / tcg::BM), p->K2p / tcg::BK, sms, p->ksg, p->kpg);
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
@@ -2168,7 +2180,8 @@ namespace {
 template <int CB>
 cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
   const int M = p->M, R = p->R, C = a.C;
-  float *U = reinterpret_cast<float *>(p->mem + p->oU);
+  const bool given = a.U_in != nullptr;
+  const float *U = given ? a.U_in : reinterpret_cast<float *>(p->mem + p->oU);
   float *Ypart = reinterpret_cast<float *>(p->mem + p->oY);
   float *G1 = reinterpret_cast<float *>(p->mem + p->oG1);
   float *G2 = C > 1 ? reinterpret_cast<float *>(p->mem + p->oG2) : nullptr;
@@ -2177,9 +2190,10 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
   float *scal = reinterpret_cast<float *>(ctl);
   unsigned *counter = reinterpret_cast<unsigned *>(ctl + 32);
   unsigned *err = reinterpret_cast<unsigned *>(ctl + 48);
-  k_prep<<<dim3((M + 127) / 128, C), 128, 0, st>>>(a, M, U, err);
+  if (!given)
+    k_prep<<<dim3((M + 127) / 128, C), 128, 0, st>>>(a, M, reinterpret_cast<float *>(p->mem + p->oU), err);
   {
-    cudaError_t e0 = obj_begin_call(err, true, st);
+    cudaError_t e0 = obj_begin_call(err, !given, st);
     if (e0 != cudaSuccess) return e0;
   }
   const long long nay = (long long)C * (p->Kp / 2);
@@ -2188,7 +2202,7 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
   dim3 gy(p->Rp / tcg::BN, p->Mp / tcg::BM, p->ksy);
   k_cgemm3<<<gy, 128, tcg::SMEM, st>>>(p->m_ayh, p->m_ayl, p->m_byh, p->m_byl, p->kpy,
                                         p->Kp / tcg::BK, C, R, R, Ypart, err);
-  const bool need_g = a.grad_W || a.grad_phi;
+  const bool need_g = a.grad_W || a.grad_phi || a.grad_U;
   if (CB >= 8) {
     constexpr int CW = CB >= 8 ? CB : 8;
     float *maxr = G1;  // G1 / G2 are not needed on this branch: per-Rx max and argmax
@@ -2223,6 +2237,15 @@ cudaError_t run_tc(ObjTcPlan *p, const ObjArgs &a, char *ctl, cudaStream_t st) {
   float *GU = reinterpret_cast<float *>(p->mem + p->oGUs);
   const long long ngu = (long long)C * p->K;
   k_gu_reduce<<<(unsigned)((ngu + 255) / 256), 256, 0, st>>>(GUp, p->ksg, ngu, GU);
+  if (given) {
+    // dL/dU is G_U's metasurface rows, dL/dW its H_d rows (poisoned like
+    // the other outputs when a wait ran out)
+    if (a.grad_U)
+      k_tc_copy_rows<<<(C * M + 255) / 256, 256, 0, st>>>(GU, p->K, 0, M, C, a.grad_U, err);
+    if (a.grad_W)
+      k_tc_copy_rows<<<(C * p->S + 255) / 256, 256, 0, st>>>(GU, p->K, M, p->S, C, a.grad_W, err);
+    return cudaGetLastError();
+  }
   if (a.grad_phi) k_tc_dphi<<<(M + 31) / 32, 256, 0, st>>>(GU, U, C, M, p->K, a.grad_phi, err);
   if (a.grad_W) {
     float *dwp = reinterpret_cast<float *>(p->mem + p->oDw);
@@ -2240,6 +2263,9 @@ cudaError_t obj_tc_run(ObjTcPlan *p, const ObjArgs &a0, cudaStream_t st) {
   ObjArgs a = a0;
   a.Hd = p->Hd; a.Ha = p->Ha; a.Hr = p->Hr;
   a.S = p->S; a.M = p->M; a.R = p->R;
+  // a coefficient-given call needs the tensor-core mode; a call that forms
+  // U from W, H_a and phi needs H_a
+  if (a.U_in ? p->stream : (p->Ha == nullptr)) return cudaErrorInvalidValue;
   if (p->stream) {
     if (a.grad_Y) return cudaErrorInvalidValue;  // not produced by the streaming kernels
     return cbucket(a.C) == 1 ? run_plan_stream<1>(p, a, st) : run_plan_stream<2>(p, a, st);
@@ -2273,6 +2299,57 @@ __global__ void k_coverage_db(const float *H, int S, int R, float threshold, flo
   out[r] = fmaxf(d, threshold);
 }
 }  // namespace
+
+namespace {
+// complex GEMM, 16 x 16 output tiles through shared memory, FP32
+__device__ __forceinline__ float2 cg_ld(const float2 *X, int ld, int op, int r, int c) {
+  // element (r, c) of op(X): 0 X, 1 X^T, 2 X^H, 3 conj(X)
+  if (op == 0) return X[(size_t)r * ld + c];
+  if (op == 3) {
+    const float2 v = X[(size_t)r * ld + c];
+    return make_float2(v.x, -v.y);
+  }
+  const float2 v = X[(size_t)c * ld + r];
+  return op == 1 ? v : make_float2(v.x, -v.y);
+}
+__global__ void __launch_bounds__(256) k_cgemm_small(int m, int n, int k, const float2 *A, int lda,
+                                                     int opA, const float2 *B, int ldb, int opB,
+                                                     float2 *C, int ldc, int accumulate) {
+  __shared__ float2 As[16][17], Bs[16][17];
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int row = blockIdx.y * 16 + ty, col = blockIdx.x * 16 + tx;
+  float2 acc = make_float2(0.f, 0.f);
+  for (int k0 = 0; k0 < k; k0 += 16) {
+    As[ty][tx] = (row < m && k0 + tx < k) ? cg_ld(A, lda, opA, row, k0 + tx) : make_float2(0.f, 0.f);
+    Bs[ty][tx] = (k0 + ty < k && col < n) ? cg_ld(B, ldb, opB, k0 + ty, col) : make_float2(0.f, 0.f);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      const float2 a = As[ty][q], b = Bs[q][tx];
+      acc.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x));
+      acc.y = fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y));
+    }
+    __syncthreads();
+  }
+  if (row < m && col < n) {
+    float2 *o = C + (size_t)row * ldc + col;
+    if (accumulate) { acc.x += o->x; acc.y += o->y; }
+    *o = acc;
+  }
+}
+}  // namespace
+
+cudaError_t cgemm_run(int m, int n, int k, const float *A, int lda, int opA, const float *B,
+                      int ldb, int opB, float *C, int ldc, bool accumulate, cudaStream_t st) {
+  if (m <= 0 || n <= 0 || k <= 0 || opA < 0 || opA > 3 || opB < 0 || opB > 3)
+    return cudaErrorInvalidValue;
+  dim3 grid((n + 15) / 16, (m + 15) / 16), block(16, 16);
+  if (grid.y > 65535u) return cudaErrorInvalidValue;
+  k_cgemm_small<<<grid, block, 0, st>>>(m, n, k, reinterpret_cast<const float2 *>(A), lda, opA,
+                                        reinterpret_cast<const float2 *>(B), ldb, opB,
+                                        reinterpret_cast<float2 *>(C), ldc, accumulate ? 1 : 0);
+  return cudaGetLastError();
+}
 
 cudaError_t coverage_db_run(const float *H, int S, int R, float threshold, float offset,
                             float *out, cudaStream_t st) {

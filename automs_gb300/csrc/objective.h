@@ -13,6 +13,11 @@ struct ObjArgs {
   float w;
   const uint8_t *drop;
   float *loss, *grad_W, *grad_phi, *recv_amp, *grad_Y;
+  // plan evaluations with the metasurface rows' coefficient given directly
+  // (U_in [C, M], instead of (W H_a) e^{j phi'}): grad_U [C, M] receives
+  // dL/dU and grad_W only the H_d rows' part
+  const float *U_in = nullptr;
+  float *grad_U = nullptr;
 };
 
 // Byte offsets of the scratch regions for one problem size.  The first 256
@@ -51,10 +56,18 @@ cudaError_t obj_noalloc_scratch(char **out);
 // evaluations on one plan must not overlap.  1 <= C <= Cmax <= 64.
 struct ObjTcPlan;
 cudaError_t obj_tc_plan_create(const float *Hd, const float *Ha, const float *Hr, int S, int M,
-                               int R, int Cmax, cudaStream_t st, ObjTcPlan **out);
+                               int R, int Cmax, cudaStream_t st, ObjTcPlan **out,
+                               bool force_tc = false);
 cudaError_t obj_tc_run(ObjTcPlan *p, const ObjArgs &a, cudaStream_t st);
 size_t obj_tc_plan_bytes(const ObjTcPlan *p);
 // device address of the plan's wait-timeout word
 const unsigned *obj_tc_plan_status_word(const ObjTcPlan *p);
 bool obj_tc_plan_streams(const ObjTcPlan *p);
 void obj_tc_plan_destroy(ObjTcPlan *p);
+
+// C = op(A) op(B) (+ C when accumulate) for row-major complex64 matrices on
+// the CUDA cores; op 0 = as is, 1 = transposed, 2 = conjugate transposed,
+// 3 = conjugated.
+// C is m x n, the inner dimension k; lda, ldb, ldc in complex elements.
+cudaError_t cgemm_run(int m, int n, int k, const float *A, int lda, int opA, const float *B,
+                      int ldb, int opB, float *C, int ldc, bool accumulate, cudaStream_t st);

@@ -133,6 +133,128 @@ def capacity_objective(W, H_d, H_a=None, H_r=None, phi=None, max_phase=2 * math.
     return (loss, recv) if return_recv else loss
 
 
+def cgemm(A, B, opA=0, opB=0, out=None, accumulate=False):
+    """op(A) op(B) (+ out) on the library's complex GEMM (ams_cgemm): 2-D
+    complex64 CUDA tensors; op 0 as is, 1 transposed, 2 conjugate
+    transposed, 3 conjugated."""
+    A, B = _c64(A), _c64(B)
+    m, k = (A.shape[0], A.shape[1]) if opA in (0, 3) else (A.shape[1], A.shape[0])
+    kb, n = (B.shape[0], B.shape[1]) if opB in (0, 3) else (B.shape[1], B.shape[0])
+    if k != kb:
+        raise ValueError(f"inner dimensions differ: {k} vs {kb}")
+    if out is None:
+        out = (torch.zeros if accumulate else torch.empty)(m, n, dtype=torch.complex64,
+                                                         device=A.device)
+    call("ams_cgemm", m, n, k, _ptr(A), A.shape[1], opA, _ptr(B), B.shape[1], opB, _ptr(out),
+         out.shape[1], int(accumulate), _stream())
+    return out
+
+
+class StackedPlan:
+    """Tensor-core objective plan over several metasurfaces'
+    channels (ams_objective_plan_create_stacked): the MS->Rx rows of every
+    metasurface stacked in one [M, R] block beside H_d."""
+
+    def __init__(self, H_d, H_rs, c_max):
+        lib()
+        self.Hd = _c64(H_d.detach())
+        self.Hr = torch.cat([_c64(h.detach()) for h in H_rs], 0).contiguous()
+        self.sizes = [h.shape[0] for h in H_rs]
+        self.S, self.R = self.Hd.shape
+        self.M = self.Hr.shape[0]
+        self.c_max = int(c_max)
+        h = C.c_void_p()
+        call("ams_objective_plan_create_stacked", _ptr(self.Hd), _ptr(self.Hr), self.S, self.M,
+             self.R, self.c_max, _stream(), C.byref(h))
+        self._h = h
+
+    close = ObjectivePlan.close
+    __del__ = ObjectivePlan.__del__
+
+
+def ms_paths(n_ms, max_ms_reflex):
+    """Metasurface sequences of get_channel (go.py:112-156): lengths 1 ..
+    max_ms_reflex, no metasurface twice in a row."""
+    out = []
+    for L in range(1, max_ms_reflex + 1):
+        for path in itertools.product(range(n_ms), repeat=L):
+            if all(path[i] != path[i + 1] for i in range(L - 1)):
+                out.append(path)
+    return out
+
+
+class MultiHopObjective(torch.autograd.Function):
+    """loss(W, phi) of go.py:107-245 for several metasurfaces and paths up to
+    max_ms_reflex hops on the library's kernels: each path's product
+    (W H_a^(p0) o e^(p0)) H^(p0 p1) o e^(p1) ... (ams_cgemm) adds to the
+    coefficient of its last metasurface's rows, one stacked tensor-core
+    evaluation (ams_objective_plan_coef_fwd_bwd) gives the loss and dL/dU,
+    and the backward pass chains dL/dU through the products (ams_cgemm)."""
+
+    @staticmethod
+    def forward(ctx, W, phi_cat, plan, chans, max_phases, paths, w, drop, want_recv):
+        Wc = _c64(W.detach())
+        Cc = Wc.shape[0]
+        off = [0]
+        for m in plan.sizes:
+            off.append(off[-1] + m)
+        e = []
+        for i, mp in enumerate(max_phases):
+            ph = torch.remainder(phi_cat.detach()[off[i]:off[i + 1]].to(torch.float32), mp)
+            e.append(torch.polar(torch.ones_like(ph), ph).to(torch.complex64))
+        U = torch.zeros(Cc, plan.M, dtype=torch.complex64, device=W.device)
+        saved = []
+        for path in paths:
+            X = cgemm(Wc, chans["src_to_ms{%d}" % path[0]])
+            V = X * e[path[0]][None, :]
+            nodes = [(path[0], V, None, 0)]
+            for prev, m in zip(path[:-1], path[1:]):
+                if prev < m:
+                    B, op = chans["ms{%d}_to_ms{%d}" % (prev, m)], 0
+                else:
+                    B, op = chans["ms{%d}_to_ms{%d}" % (m, prev)], 1
+                X = cgemm(V, B, opB=op)
+                V = X * e[m][None, :]
+                nodes.append((m, V, B, op))
+            last = path[-1]
+            U[:, off[last]:off[last + 1]] += V
+            saved.append((path, nodes))
+        loss = torch.empty((), dtype=torch.float32, device=W.device)
+        gU = torch.empty_like(U)
+        gW = torch.empty_like(Wc)
+        recv = torch.empty(Cc, plan.R, dtype=torch.float32, device=W.device) if want_recv else None
+        dr = drop.to(device=W.device, dtype=torch.uint8).contiguous() if drop is not None else None
+        call("ams_objective_plan_coef_fwd_bwd", plan._h, _ptr(U), _ptr(Wc), Cc, float(w), _ptr(dr),
+             _ptr(loss), _ptr(gU), _ptr(gW), _ptr(recv), _stream())
+        ctx.saved = (saved, e, off, chans)
+        ctx.save_for_backward(gU, gW)
+        ctx.w_dtype = W.dtype
+        if recv is not None:
+            ctx.mark_non_differentiable(recv)
+            return loss, recv
+        return loss, torch.empty(0, device=W.device)
+
+    @staticmethod
+    def backward(ctx, gl, _grecv):
+        gU, gW = ctx.saved_tensors
+        saved, e, off, chans = ctx.saved
+        dW = gW * gl
+        dphi = torch.zeros(off[-1], dtype=torch.float32, device=gU.device)
+        for path, nodes in saved:
+            last = path[-1]
+            dV = gU[:, off[last]:off[last + 1]] * gl
+            for k in range(len(nodes) - 1, -1, -1):
+                m, V, B, op = nodes[k]
+                dphi[off[m]:off[m + 1]] -= torch.imag(torch.conj(dV) * V).sum(0)
+                dX = dV * torch.conj(e[m])[None, :]
+                if k > 0:
+                    # X = V_prev B (op 0) or V_prev B^T (op 1)
+                    dV = cgemm(dX, B, opB=2 if op == 0 else 3)
+                else:
+                    dW = dW + cgemm(dX, chans["src_to_ms{%d}" % m], opB=2)
+        return (dW.to(ctx.w_dtype), dphi, None, None, None, None, None, None, None)
+
+
 def check_status(plan=None):
     """Raise AmsError if a bounded wait of the last objective call ran out
     (its outputs are then NaN): the last call on `plan`, or with plan=None the
@@ -215,7 +337,9 @@ class Model(nn.Module):
         return n == 0 or self.max_ms_reflex == 0 or (n == 1 and self.max_ms_reflex >= 1)
 
     def get_channel(self):
-        """Composite channel H [S, R] (go.py:107-157), in torch."""
+        """Composite channel H [S, R] (go.py:107-157), the path products on
+        the library's complex GEMM (not differentiable: forward() forms the
+        loss and its gradient without it)."""
         channel = self.pick_channel(True)["src_to_dst"]
         for L in range(1, self.max_ms_reflex + 1):
             for path in itertools.product(range(len(self.ms_list)), repeat=L):
@@ -223,14 +347,17 @@ class Model(nn.Module):
                     continue
                 msc = self.pick_channel()["src_to_ms{%d}" % path[0]]
                 for i, m in enumerate(path):
-                    real = self.ms_theta[m] % self.ms_list[m].max_phase
+                    real = self.ms_theta[m].detach() % self.ms_list[m].max_phase
                     msc = msc * (self.ms_A[m] * torch.exp(1j * real))
                     if i == L - 1:
-                        msc = msc @ self.pick_channel()["ms{%d}_to_dst" % m]
+                        msc = cgemm(msc, self.pick_channel()["ms{%d}_to_dst" % m])
                     else:
                         nx = path[i + 1]
-                        msc = msc @ (self.pick_channel()["ms{%d}_to_ms{%d}" % (m, nx)] if m < nx
-                                     else self.pick_channel()["ms{%d}_to_ms{%d}" % (nx, m)].T)
+                        if m < nx:
+                            msc = cgemm(msc, self.pick_channel()["ms{%d}_to_ms{%d}" % (m, nx)])
+                        else:
+                            msc = cgemm(msc, self.pick_channel()["ms{%d}_to_ms{%d}" % (nx, m)],
+                                        opB=1)
                 channel = channel + msc
         return channel
 
@@ -256,8 +383,19 @@ class Model(nn.Module):
                 loss, recv = capacity_objective(W, ch["src_to_dst"], w=self.w, drop=drop,
                                                 return_recv=True)
         else:
-            H = self.get_channel()
-            loss, recv = capacity_objective(W, H, w=self.w, drop=drop, return_recv=True)
+            # several metasurfaces / hops: path products on the library's
+            # complex GEMM, one stacked tensor-core evaluation
+            ch = self.pick_channel(True)
+            n = len(self.ms_list)
+            plan = self._plans.get(("stacked", id(ch)))
+            if plan is None:
+                plan = StackedPlan(ch["src_to_dst"], [ch["ms{%d}_to_dst" % i] for i in range(n)],
+                                   c_max=C_)
+                self._plans[("stacked", id(ch))] = plan
+            loss, recv = MultiHopObjective.apply(
+                W, torch.cat(list(self.ms_theta)), plan, ch,
+                [m.max_phase for m in self.ms_list], ms_paths(n, self.max_ms_reflex), self.w,
+                drop, True)
         self.result = recv.detach().clone()
         self.max_code_ids = recv.max(0)[1].detach().clone()
         eps = torch.finfo(torch.float32).eps

@@ -205,6 +205,41 @@ ams_status ams_objective_plan_fwd_bwd(ams_objective_plan *plan,
                                       void *stream, char *errbuf,
                                       size_t errlen);
 unsigned long long ams_objective_plan_bytes(const ams_objective_plan *plan);
+
+/* Plan over a stacked channel set for several metasurfaces: H_r [M, R]
+ * holds the rows of every metasurface's MS->Rx channel one after the other
+ * (M = the sum of their sizes), H_d [S, R] the AP->Rx channel; tensor-core
+ * mode (3xBF16) whatever C_max.  Its evaluations take the coefficient of
+ * every metasurface row directly, U [C, M] complex: the sum over all
+ * metasurface paths that end on that element of the path product up to it
+ * (go.py:112-156; for one metasurface U = (W H_a) o e^{j phi'}), so that
+ *   Y = W H_d + U H_r
+ * and the loss is that of ams_objective_fwd_bwd.  Outputs: loss, grad_U
+ * [C, M] (dL/dU, complex convention of grad_W), grad_W [C, S] (the H_d
+ * term only), recv_amp [C, R]; any but loss may be NULL.  The caller chains
+ * grad_U back through its path products (ams_cgemm). */
+ams_status ams_objective_plan_create_stacked(const float *H_d, const float *H_r,
+                                             int S, int M, int R, int C_max,
+                                             void *stream,
+                                             ams_objective_plan **out,
+                                             char *errbuf, size_t errlen);
+ams_status ams_objective_plan_coef_fwd_bwd(ams_objective_plan *plan,
+                                           const float *U, const float *W,
+                                           int C, float w, const uint8_t *drop,
+                                           float *loss, float *grad_U,
+                                           float *grad_W, float *recv_amp,
+                                           void *stream, char *errbuf,
+                                           size_t errlen);
+
+/* C = op(A) op(B) (+ C when accumulate != 0) for row-major complex64
+ * device matrices (interleaved float pairs) on the CUDA cores, FP32: op 0
+ * as is, 1 transposed, 2 conjugate transposed, 3 conjugated; C is m x n, k the inner
+ * dimension, lda/ldb/ldc in complex elements.  The path products between
+ * metasurfaces of go.py:138-146 and their adjoints (small: C codes by the
+ * metasurface sizes). */
+ams_status ams_cgemm(int m, int n, int k, const float *A, int lda, int opA,
+                     const float *B, int ldb, int opB, float *C, int ldc,
+                     int accumulate, void *stream, char *errbuf, size_t errlen);
 void ams_objective_plan_destroy(ams_objective_plan *plan);
 
 /* Wait-timeout report of the objective.  The streaming and tensor-core

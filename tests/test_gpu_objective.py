@@ -79,7 +79,16 @@ def test_model_matches_reference_model(obj, name):
         loss = obj.capacity_objective(W, ch["src_to_dst"], args[0], args[1], args[2], args[3],
                                       c["w"], cuda(g["drop"]))
     else:
-        loss = obj.capacity_objective(W, m.get_channel(), w=c["w"], drop=cuda(g["drop"]))
+        # several metasurfaces: Model.forward (library path products and the
+        # stacked tensor-core evaluation) with the reference's dropout rows
+        m.drop_rate = 0.1
+        mask = torch.from_numpy(np.where(g["drop"], 0.0, 0.5).astype(np.float32))
+        real_rand = torch.rand
+        torch.rand = lambda *a, **k: mask.clone()
+        try:
+            loss = m.forward()
+        finally:
+            torch.rand = real_rand
     loss.backward()
     np.testing.assert_allclose(float(loss), float(g["loss"]), rtol=2e-4)
     gt = g["grad_theta"]
@@ -399,3 +408,104 @@ def test_postprocess_matches_reference_model(obj, name, monkeypatch):
     assert clear.mean() > 0.9
     np.testing.assert_array_equal(ids[clear], g["max_code_ids"][clear])
     np.testing.assert_allclose(float(m.loss), float(g["loss"]), rtol=2e-4)
+
+
+def _reference_multihop_loss(torch_, ch, W, phis, max_phases, reflex, w, drop):
+    """go.py:107-157 get_channel + go.py:159-226 forward (capacity mode) in
+    float64 / complex128 on the CPU with autograd: the reference's method."""
+    import itertools
+    n = len(phis)
+    H = ch["src_to_dst"]
+    for L in range(1, reflex + 1):
+        for path in itertools.product(range(n), repeat=L):
+            if any(path[i] == path[i + 1] for i in range(L - 1)):
+                continue
+            msc = ch["src_to_ms{%d}" % path[0]]
+            for i, m in enumerate(path):
+                msc = msc * torch_.exp(1j * torch_.remainder(phis[m], max_phases[m]))
+                if i == L - 1:
+                    msc = msc @ ch["ms{%d}_to_dst" % m]
+                else:
+                    nx = path[i + 1]
+                    msc = msc @ (ch["ms{%d}_to_ms{%d}" % (m, nx)] if m < nx
+                                 else ch["ms{%d}_to_ms{%d}" % (nx, m)].T)
+            H = H + msc
+    Y = W @ H
+    cap = torch_.log2(1.0 + (Y.abs() + OO.EPS32) ** 2 / OO.N0)
+    cap = cap * (~drop)[:, None]
+    mx, _ = cap.max(0)
+    masked = cap * (cap != mx[None, :])
+    return -w * mx.sum() + torch_.linalg.norm(masked)
+
+
+def test_multihop_objective_vs_reference_autograd(obj):
+    """Three metasurfaces, paths of up to three hops (transposed hops
+    included): loss and gradients of Model.forward (library path products +
+    stacked tensor-core evaluation) against the reference's method in
+    float64 with autograd."""
+    from automs_gb300.geometry import Metasurface
+    rng = np.random.Generator(np.random.PCG64(77))
+    S, R, C, Ms = 8, 300, 6, [40, 24, 32]
+    ch = {"src_to_dst": cases._cn(rng, (S, R))}
+    for i, M in enumerate(Ms):
+        ch["src_to_ms{%d}" % i] = cases._cn(rng, (S, M)) * 30
+        ch["ms{%d}_to_dst" % i] = cases._cn(rng, (M, R)) * 30
+    for i in range(3):
+        for j in range(i + 1, 3):
+            ch["ms{%d}_to_ms{%d}" % (i, j)] = cases._cn(rng, (Ms[i], Ms[j])) * 30
+    theta = rng.uniform(0, 2 * np.pi, size=(C, S)).astype(np.float32)
+    phis = [rng.uniform(0, 4 * np.pi, size=M).astype(np.float32) for M in Ms]
+    max_deg = [360.0, 300.0, 270.0]
+    drop = np.zeros(C, bool)
+    drop[2] = True
+    ms = [Metasurface(None, None, None, None, None, d) for d in max_deg]
+    m = obj.Model("t", {k: cuda(v) for k, v in ch.items()}, ms, max_ms_reflex=3, code_num=C,
+                  w=0.7, drop_rate=0.1)
+    with torch.no_grad():
+        m.antenna_theta.copy_(cuda(theta))
+        for i in range(3):
+            m.ms_theta[i].copy_(cuda(phis[i]))
+    for p in m.parameters():
+        p.grad = None
+    mask = torch.from_numpy(np.where(drop, 0.0, 0.5).astype(np.float32))
+    real_rand = torch.rand
+    torch.rand = lambda *a, **k: mask.clone()
+    try:
+        loss = m.forward()
+    finally:
+        torch.rand = real_rand
+    loss.backward()
+    obj.check_status()
+    # reference: float64 autograd on the CPU
+    t64 = {k: torch.from_numpy(v.astype(np.complex128)) for k, v in ch.items()}
+    th = torch.from_numpy(theta.astype(np.float64)).requires_grad_(True)
+    ph = [torch.from_numpy(p.astype(np.float64)).requires_grad_(True) for p in phis]
+    A = torch.from_numpy(OO.antenna_amplitude(C, S))
+    W64 = A * torch.exp(-1j * th)
+    ref = _reference_multihop_loss(torch, t64, W64, ph, [d / 180 * np.pi for d in max_deg], 3,
+                                   0.7, torch.from_numpy(drop))
+    ref.backward()
+    np.testing.assert_allclose(float(loss), float(ref), rtol=1e-4)
+    gt = th.grad.numpy()
+    np.testing.assert_allclose(m.antenna_theta.grad.cpu().numpy(), gt, rtol=1e-3,
+                               atol=1e-3 * np.abs(gt).max())
+    for i in range(3):
+        gp = ph[i].grad.numpy()
+        np.testing.assert_allclose(m.ms_theta[i].grad.cpu().numpy(), gp, rtol=1e-3,
+                                   atol=1e-3 * np.abs(gp).max())
+
+
+def test_cgemm_ops(obj):
+    """ams_cgemm against numpy for each operand mode, with accumulation."""
+    rng = np.random.Generator(np.random.PCG64(5))
+    mk = lambda *sh: (rng.normal(size=sh) + 1j * rng.normal(size=sh)).astype(np.complex64)
+    f = {0: lambda x: x, 1: lambda x: x.T, 2: lambda x: x.conj().T, 3: lambda x: x.conj()}
+    for opA in range(4):
+        for opB in range(4):
+            A = mk(37, 50) if opA in (0, 3) else mk(50, 37)
+            B = mk(50, 29) if opB in (0, 3) else mk(29, 50)
+            C0 = mk(37, 29)
+            out = cuda(C0)
+            obj.cgemm(cuda(A), cuda(B), opA, opB, out=out, accumulate=True)
+            ref = C0.astype(np.complex128) + f[opA](A).astype(np.complex128) @ f[opB](B)
+            np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-4, atol=1e-4 * np.abs(ref).max())
