@@ -65,6 +65,9 @@ SIGNATURES = {
                                   _I, _I, _P, _I, _P, _P, _I, _I, _I, _I, _D, _D,
                                   C.POINTER(Stats), _E, _S]),
     "ams_trace_export_paths": (_I, [_P, _P, _I, C.POINTER(_I), _E, _S]),
+    "ams_trace_channel_export": (_I, [_P, C.POINTER(TraceParams), _P, _I, _I, _P, _I, _I, _P, _P,
+                                      _P, C.POINTER(Stats), _P, C.c_ulonglong,
+                                      C.POINTER(C.c_ulonglong), _P, _E, _S]),
     "ams_objective_fwd_bwd": (_I, [_P, _P, _P, _P, _F, _P, _I, _I, _I, _I, _F, _P, _P, _P, _P,
                                    _P, _P, _P, _E, _S]),
     "ams_objective_fwd_bwd_noalloc": (_I, [_P, _P, _P, _P, _F, _P, _I, _I, _I, _I, _F, _P, _P,

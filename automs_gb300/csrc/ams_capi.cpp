@@ -367,10 +367,17 @@ static ams_status validate(const ams_trace_params *p, int s0, int s1, int n0, in
   return AMS_OK;
 }
 
-ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const float *src, int s0,
-                             int s1, const float *dst, int n0, int n1, const float *src_aabb_in,
-                             const float *dst_aabb_in, float *result, ams_stats *stats,
-                             void *stream, char *errbuf, size_t errlen) {
+}  // extern "C"
+
+namespace {
+// The trace of ams_trace_channel; with records != nullptr, every backward
+// ray's record is written (one path per stage-2 item in every round).
+ams_status trace_impl(ams_scene *S, const ams_trace_params *p, const float *src, int s0, int s1,
+                      const float *dst, int n0, int n1, const float *src_aabb_in,
+                      const float *dst_aabb_in, float *result, ams_stats *stats,
+                      ams_ray_record *records, unsigned long long max_records,
+                      unsigned long long *n_records, void *stream, char *errbuf,
+                      size_t errlen) {
   clear_stale_error();
   if (!S) { set_err(errbuf, errlen, "scene is NULL"); return AMS_ERR_ARG; }
   ams_status v = validate(p, s0, s1, n0, n1, errbuf, errlen);
@@ -406,6 +413,9 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
     char *tx_out = S->ws.take<char>(lbvh_output_bytes(n_src));
     char *rx_out = S->ws.take<char>(lbvh_output_bytes(n_dst));
     TraceDev P{};
+    P.rec = records;
+    P.rec_cap = records ? max_records : 0;
+    P.rec_base = 0;
     P.tab_h = S->ws.take<unsigned long long>(tab_size);
     P.tab_key = S->ws.take<int32_t>(14 * (size_t)tab_size);
     P.T = S->ws.take<unsigned>((size_t)ng * W);
@@ -503,10 +513,15 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
         P.task_cap = (S->tasks.cap - 512) / per_task;
         P.task_path = reinterpret_cast<int2 *>(S->tasks.base);
         P.chunk_at = reinterpret_cast<int4 *>(S->tasks.base + al(sizeof(int2) * P.task_cap));
-        P.kpi = trace_paths_per_item(P, n_new);
+        P.kpi = records ? 1 : trace_paths_per_item(P, n_new);
         CK(trace_make_tasks(P, P.N, st));
         CK(cudaEventRecord(S->k2[0], st));
-        CK(trace_stage2(P, n_new, st));
+        if (records) {
+          CK(trace_stage2_export(P, n_new, st));
+          P.rec_base += n_new * (unsigned long long)(gs * gs) * (unsigned long long)n_src;
+        } else {
+          CK(trace_stage2(P, n_new, st));
+        }
         CK(cudaEventRecord(S->k2[1], st));
         CK(trace_expand(P, st));
         rounds++;
@@ -552,6 +567,7 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
       stats->segments_bwd = S->hc->ctr[9];
       stats->ms_stage2_kernel = ms_k2;
     }
+    if (n_records) *n_records = P.rec_base;
     if (p->log_level > 0) {
       const float a = elapsed_ms(ev[0], ev[1]), b = elapsed_ms(ev[1], ev[2]),
                   c = elapsed_ms(ev[2], ev[3]);
@@ -565,6 +581,33 @@ ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const floa
   }
   set_err(errbuf, errlen, "path table retries exhausted");
   return AMS_ERR_CAPACITY;
+}
+}  // namespace
+
+extern "C" {
+
+ams_status ams_trace_channel(ams_scene *S, const ams_trace_params *p, const float *src, int s0,
+                             int s1, const float *dst, int n0, int n1, const float *src_aabb,
+                             const float *dst_aabb, float *result, ams_stats *stats,
+                             void *stream, char *errbuf, size_t errlen) {
+  return trace_impl(S, p, src, s0, s1, dst, n0, n1, src_aabb, dst_aabb, result, stats, nullptr, 0,
+                    nullptr, stream, errbuf, errlen);
+}
+
+ams_status ams_trace_channel_export(ams_scene *S, const ams_trace_params *p, const float *src,
+                                    int s0, int s1, const float *dst, int n0, int n1,
+                                    const float *src_aabb, const float *dst_aabb, float *result,
+                                    ams_stats *stats, ams_ray_record *records,
+                                    unsigned long long max_records,
+                                    unsigned long long *n_records, void *stream, char *errbuf,
+                                    size_t errlen) {
+  if (!records || !n_records) {
+    set_err(errbuf, errlen, "records and n_records are required");
+    return AMS_ERR_ARG;
+  }
+  *n_records = 0;
+  return trace_impl(S, p, src, s0, s1, dst, n0, n1, src_aabb, dst_aabb, result, stats, records,
+                    max_records, n_records, stream, errbuf, errlen);
 }
 
 ams_status ams_launch_pathtrace(float *result, const float *src, int s0, int s1, const float *dst,

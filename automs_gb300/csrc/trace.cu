@@ -980,9 +980,10 @@ __global__ void k_cell_fill(TraceDev P, const unsigned *bits) {
 // optixPathTracer.cu:191-273, :332-417): the image source of the path key in
 // `slot` seen from Rx position o, traced back to Tx `s`.  Returns true with
 // the contribution as 2^-56 fixed point when the ray arrives.
+template <bool EXPORT = false>
 __device__ __forceinline__ bool s2_ray(const TraceDev &P, int slot, int s, af3 o, af3 srcdir,
                                        af3 dstdir, unsigned &segs, unsigned long long &cre,
-                                       unsigned long long &cim) {
+                                       unsigned long long &cim, ams_ray_record *rr = nullptr) {
   const int32_t *key = P.tab_key + (size_t)slot * 14;
   Mat34 M;
 #pragma unroll
@@ -991,6 +992,11 @@ __device__ __forceinline__ bool s2_ray(const TraceDev &P, int slot, int s, af3 o
   const float lam = P.lam_f;
   af3 d = nrm3(sub3(image_of(M, ld3(P.src + 3 * s)), o));
   float amp = beampattern(d, dstdir, P.dst_bp);
+  float xloss = 1.0f;  // exported: free-space factors only
+  if (EXPORT) {
+    rr->receive_angle = dot3(d, dstdir) / (len3(d) * len3(dstdir));
+    rr->hit_cnt = 0;
+  }
   float far = 1e6f, dd = 0.0f, dres = 0.0f;
   double D = 0.0;
   int ttl = hc + 1;
@@ -1022,6 +1028,11 @@ __device__ __forceinline__ bool s2_ray(const TraceDev &P, int slot, int s, af3 o
       if (dd > far) { fspl = lam / ((4.0f * AMS_PIF) * dres); dres = 0.0f; }
       amp *= loss * fspl;
       dres += dd;
+      if (EXPORT) {
+        if (rr->hit_cnt < 5) rr->hit_loss_idx[rr->hit_cnt] = theta_id(ct) + m * AMS_NBINS;
+        rr->hit_cnt++;
+        xloss *= fspl;
+      }
       // far_dist = 2 max_d^2 / lambda, divided in double and rounded to
       // float (optixPathTracer.cu:385-389).  Its value matters only when
       // the segment is longer; a float estimate (relative error < 3e-7)
@@ -1041,6 +1052,12 @@ __device__ __forceinline__ bool s2_ray(const TraceDev &P, int slot, int s, af3 o
         float af = lam / ((4.0f * AMS_PIF) * (dres + dd));
         amp *= bp * af;
         ok = true;
+        if (EXPORT) {
+          const af3 nd = neg3(d);
+          rr->launch_angle = dot3(nd, srcdir) / (len3(nd) * len3(srcdir));
+          rr->loss = xloss * af;
+          rr->phase = D * P.two_pi_over_lam;
+        }
       }
       break;
     }
@@ -1144,6 +1161,7 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
 // rays of all tasks laid out back to back (task-major, then Rx within the
 // cell, then Tx), so no warp idles on the padding of a task's last item.
 // Each verified ray adds its contribution to the Rx-major accumulator.
+template <bool EXPORT>
 __global__ void __launch_bounds__(256, 5) k_stage2_rays(TraceDev P) {
   const int S = P.n_src;
   const long long pairs = (long long)P.gs * P.gs * S;
@@ -1173,22 +1191,37 @@ __global__ void __launch_bounds__(256, 5) k_stage2_rays(TraceDev P) {
   }
   bool ok = false, traced = false;
   unsigned segs = 0;
+  ams_ray_record rr;
+  if (EXPORT) {
+    rr.src = s; rr.dst = -1; rr.path = path; rr.traced = 0; rr.successful = 0; rr.hit_cnt = 0;
+    rr.launch_angle = 0.f; rr.receive_angle = 0.f; rr.loss = 0.f; rr.pad0 = 0.f;
+    rr.phase = 0.0; rr.pad1 = 0;
+#pragma unroll
+    for (int i = 0; i < 5; i++) rr.hit_loss_idx[i] = -1;
+  }
   if (valid) {
     const int gi = cell / P.n1g, gj = cell % P.n1g;
     const int di = inner / P.gs + gi * P.gs, dj = inner % P.gs + gj * P.gs;
     const int dst = di * P.n1_dst + dj;
+    if (EXPORT) rr.dst = dst;
     if (!(dst >= P.n_dst || (P.strict_grid && (di >= P.n0_dst || dj >= P.n1_dst)))) {
       traced = true;
       unsigned long long cre = 0, cim = 0;
       const af3 srcdir = mk3(P.src_dir[0], P.src_dir[1], P.src_dir[2]);
       const af3 dstdir = mk3(P.dst_dir[0], P.dst_dir[1], P.dst_dir[2]);
-      ok = s2_ray(P, slot, s, ld3(P.dst + 3 * dst), srcdir, dstdir, segs, cre, cim);
+      ok = s2_ray<EXPORT>(P, slot, s, ld3(P.dst + 3 * dst), srcdir, dstdir, segs, cre, cim, &rr);
       if (ok) {
         unsigned long long *acc = P.acc + ((size_t)dst * S + s) * 2;
         atomicAdd(acc, cre);
         atomicAdd(acc + 1, cim);
       }
     }
+  }
+  if (EXPORT && valid) {
+    rr.traced = traced ? 1 : 0;
+    rr.successful = ok ? 1 : 0;
+    const unsigned long long at = P.rec_base + (unsigned long long)ray;
+    if (at < P.rec_cap) P.rec[at] = rr;
   }
   // counters and each task's success bit, one atomic per warp / task
   const unsigned okb = __ballot_sync(0xffffffffu, ok);
@@ -1375,13 +1408,23 @@ cudaError_t trace_stage2(const TraceDev &P, unsigned long long n_tasks, cudaStre
   if (P.kpi == 1) {  // one path per item: one thread per ray
     const unsigned long long blocks = (n_tasks * pairs + 255) / 256;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
-    k_stage2_rays<<<(unsigned)blocks, 256, 0, st>>>(P);
+    k_stage2_rays<false><<<(unsigned)blocks, 256, 0, st>>>(P);
     return cudaGetLastError();
   }
   const unsigned long long items_max = chunks * ((pairs + 31) / 32);
   const unsigned long long blocks = (items_max + 7) / 8;
   if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
   k_stage2<<<(unsigned)blocks, 256, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t trace_stage2_export(const TraceDev &P, unsigned long long n_tasks, cudaStream_t st) {
+  if (n_tasks == 0) return cudaSuccess;
+  if (P.kpi != 1) return cudaErrorInvalidValue;
+  const unsigned long long pairs = (unsigned long long)(P.gs * P.gs) * P.n_src;
+  const unsigned long long blocks = (n_tasks * pairs + 255) / 256;
+  if (blocks > 0x7fffffffull) return cudaErrorInvalidConfiguration;
+  k_stage2_rays<true><<<(unsigned)blocks, 256, 0, st>>>(P);
   return cudaGetLastError();
 }
 

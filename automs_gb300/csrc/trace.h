@@ -3,6 +3,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/ams.h"
 #include "lbvh.h"
 
 // device error flags (bits of TraceDev::err)
@@ -75,6 +76,10 @@ struct TraceDev {
   // 10 stage-1 launch-index fetch, 12 dense path ids
   unsigned long long *ctr;
   unsigned *err;
+  // per-ray records of stage 2 (ams_trace_channel_export): record of ray r
+  // of the round at rec[rec_base + r] while below rec_cap
+  ams_ray_record *rec;
+  unsigned long long rec_cap, rec_base;
 };
 
 cudaError_t trace_stage1(const TraceDev &P, cudaStream_t st);
@@ -90,6 +95,8 @@ cudaError_t trace_count_tasks(const TraceDev &P, const unsigned *bits, cudaStrea
 // the round's task and chunk lists; also clears the success bitmap
 cudaError_t trace_make_tasks(const TraceDev &P, const unsigned *bits, cudaStream_t st);
 cudaError_t trace_stage2(const TraceDev &P, unsigned long long n_tasks, cudaStream_t st);
+// one thread per ray, each ray's record written (P.rec; P.kpi must be 1)
+cudaError_t trace_stage2_export(const TraceDev &P, unsigned long long n_tasks, cudaStream_t st);
 cudaError_t trace_expand(const TraceDev &P, cudaStream_t st);
 cudaError_t trace_count_bits(const TraceDev &P, const unsigned *bits, unsigned long long *out,
                              cudaStream_t st);

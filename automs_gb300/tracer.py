@@ -114,6 +114,33 @@ class Scene:
              _ptr(sa), _ptr(da), _ptr(result), C.byref(st), _stream())
         return result, st.as_dict()
 
+    def trace_export(self, src, dst, params, max_records=None):
+        """trace() with every backward ray of stage 2 recorded (the
+        reference's EXPORT_TASKINFO dump, optixPathTracer.h:40-52): returns
+        (result, stats, records) with records a numpy structured array of
+        RAY_RECORD (see ams_ray_record in include/ams.h), in round, task, Rx,
+        Tx order.  max_records defaults to what a first plain trace counts."""
+        if isinstance(params, dict):
+            params = params_from_dict(params)
+        if max_records is None:
+            _, st = self.trace(src, dst, params)
+            max_records = st["rx_paths"] + st["rx_fail"]
+            max_records = max(int(max_records * 1.5) + 1024, 1024)
+        src = _f32(src)
+        dst = _f32(dst)
+        s0, s1 = src.shape[0], src.shape[1]
+        n0, n1 = dst.shape[0], dst.shape[1]
+        result = torch.zeros(s0 * s1, n0 * n1, 2, dtype=torch.float32, device="cuda")
+        rec = torch.empty(int(max_records) * RAY_RECORD.itemsize, dtype=torch.uint8, device="cuda")
+        n = C.c_ulonglong()
+        st = Stats()
+        call("ams_trace_channel_export", self._h, C.byref(params), _ptr(src), s0, s1, _ptr(dst),
+             n0, n1, C.c_void_p(0), C.c_void_p(0), _ptr(result), C.byref(st), _ptr(rec),
+             C.c_ulonglong(int(max_records)), C.byref(n), _stream())
+        k = min(int(n.value), int(max_records))
+        out = rec[:k * RAY_RECORD.itemsize].cpu().numpy().view(RAY_RECORD)
+        return result, st.as_dict(), out
+
     def export_paths(self, max_paths=1 << 22):
         """Unique path keys of the last trace, int32 [P, 14], sorted in the
         order of the reference's std::map<Path, int> (optixPathTracer.h:28-38)."""
@@ -122,6 +149,14 @@ class Scene:
         out = np.zeros((max(n.value, 1), 14), np.int32)
         call("ams_trace_export_paths", self._h, C.c_void_p(out.ctypes.data), n.value, C.byref(n))
         return sort_paths(out[: n.value])
+
+
+# ams_ray_record of include/ams.h (64 bytes)
+RAY_RECORD = np.dtype([("src", "<i4"), ("dst", "<i4"), ("path", "<i4"), ("traced", "<i4"),
+                       ("successful", "<i4"), ("hit_cnt", "<i4"), ("launch_angle", "<f4"),
+                       ("receive_angle", "<f4"), ("loss", "<f4"), ("pad0", "<f4"),
+                       ("phase", "<f8"), ("hit_loss_idx", "<i4", 5), ("pad1", "<i4")])
+assert RAY_RECORD.itemsize == 64
 
 
 def sort_paths(paths):

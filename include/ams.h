@@ -118,6 +118,40 @@ ams_status ams_launch_pathtrace(
     int dst_bptype, int dst_gridsize, double src_r, double dst_r,
     ams_stats *stats, char *errbuf, size_t errlen);
 
+/* One backward ray of stage 2, as the reference's EXPORT_TASKINFO build
+ * records it (ExportedTaskInfo, optixPathTracer.h:40-52, filled at
+ * optixPathTracer.cu:200-268, 378-413): whether it reached its Tx; the
+ * cosines at the Tx (launch_angle, against src_dir) and at the Rx
+ * (receive_angle, against dst_dir); loss = the product of the free-space
+ * factors (far-field splits and lambda / (4 pi d)), material losses left
+ * out; phase = 2 pi d / lambda of the whole path (radians, unreduced; FP64
+ * here, FP32 in the reference); the Tx, the Rx, the scene hits and, per
+ * hit, theta_id + 19 * material (the mat_prop entry of its loss).  Here
+ * also the path id and whether the ray was traced (its Rx exists). */
+typedef struct {
+  int32_t src, dst, path, traced;
+  int32_t successful, hit_cnt;
+  float launch_angle, receive_angle, loss, pad0;
+  double phase;
+  int32_t hit_loss_idx[5];
+  int32_t pad1;
+} ams_ray_record; /* 64 bytes */
+
+/* ams_trace_channel, and every backward ray of stage 2 written to records
+ * (device, capacity max_records; rays past it are counted, not written) in
+ * round order, then task order (cells in order, paths within a cell), then
+ * Rx within the cell, then Tx.  *n_records receives the number of rays.
+ * Slower than ams_trace_channel (one thread per ray in every round). */
+ams_status ams_trace_channel_export(ams_scene *scene, const ams_trace_params *p,
+                                    const float *src, int s0, int s1,
+                                    const float *dst, int n0, int n1,
+                                    const float *src_aabb, const float *dst_aabb,
+                                    float *result, ams_stats *stats,
+                                    ams_ray_record *records,
+                                    unsigned long long max_records,
+                                    unsigned long long *n_records, void *stream,
+                                    char *errbuf, size_t errlen);
+
 /* Path list of the scene's last build: 14 int32 words per path (12 floats
  * of the image transform, hit count, reflect mask; optixPathTracer.h:9-13),
  * unordered, into host memory.  *n_out receives the number of paths. */

@@ -254,3 +254,54 @@ def test_building_sah_parity_with_oracle(tracer, L):
              reserve_size=100, src_bptype=2, dst_bptype=0, dst_gridsize=5, src_r=0.5e-5,
              dst_r=0.06, src_dir=[0.0, 1.0, 0.0], dst_dir=[0.0, 0.0, 0.0])
     _exact_parity(tracer, dict(tris=tris, mat=mat, mat_prop=mp, src=src, dst=dst, params=p))
+
+
+def _bp_from_cos(c, t):
+    """get_beampattern_factor (optixPathTracer.cu:107-136) of a cosine."""
+    c = np.asarray(c, np.float64)
+    if t == 0:
+        return np.ones_like(c)
+    if t == 1:
+        return np.where(c < 0, 0.0, c * 2.4495)
+    if t == 3:
+        return np.where(c < 0, 0.0, 1.4142)
+    th = np.arccos(np.clip(c, -1, 1))
+    taper = 10 ** ((2.0943951 - th) * 0.31830987 * 4.0 * 0.41299623 - 1.0) * 2.4495
+    return np.where(c < -0.5, 0.1, np.where(c < 0.25881904510252074, taper, c * 2.4495))
+
+
+@pytest.mark.parametrize("name", ["pen_l3", "ms_to_rx", "farfield"])
+def test_ray_export_rebuilds_the_channel(tracer, name):
+    """Per-ray records of stage 2 (the reference's EXPORT_TASKINFO dump): the
+    exporting trace gives the same H and counters as a plain one, the
+    records count every traced / verified ray, and H rebuilt from the
+    records (beam patterns of the cosines, the material losses of the hit
+    indices, the free-space factors, the phase) equals the traced H."""
+    c = cases.channel_case(name)
+    p = c["params"]
+    sc = tracer.Scene(c["tris"], c["mat"], c["mat_prop"])
+    r0, s0 = sc.trace(c["src"], c["dst"], p)
+    r1, s1, rec = sc.trace_export(c["src"], c["dst"], p)
+    sc.close()
+    for k in cases.STAT_KEYS + ("tasks",):
+        assert s0[k] == s1[k], k
+    assert torch.equal(r0, r1)
+    assert int(rec["successful"].sum()) == s1["rx_paths"]
+    assert int(((rec["traced"] == 1) & (rec["successful"] == 0)).sum()) == s1["rx_fail"]
+    ok = rec[rec["successful"] == 1]
+    assert (ok["hit_cnt"] <= p["max_reflection"]).all()
+    mp = np.abs(c["mat_prop"].reshape(-1).astype(np.float64))
+    mat_loss = np.ones(len(ok))
+    for h in range(5):
+        idx = ok["hit_loss_idx"][:, h]
+        use = h < ok["hit_cnt"]
+        mat_loss[use] *= mp[idx[use]]
+    amp = (_bp_from_cos(ok["receive_angle"], p["dst_bptype"]) * mat_loss * ok["loss"] *
+           _bp_from_cos(ok["launch_angle"], p["src_bptype"]))
+    H = np.zeros(r1.shape[:2], np.complex128)
+    np.add.at(H, (ok["src"], ok["dst"]), amp * np.exp(-1j * ok["phase"]))
+    Ht = (r1[..., 0] + 1j * r1[..., 1]).cpu().numpy()
+    assert rel(H, Ht) < 1e-5
+    if name == "farfield":  # some verified rays took the far-field split
+        lam = p["wave_len"]
+        assert s1["rx_paths"] > 0 and (ok["loss"] > 0).all()
