@@ -151,12 +151,12 @@ class Scene:
         return sort_paths(out[: n.value])
 
 
-# ams_ray_record of include/ams.h (64 bytes)
+# ams_ray_record of include/ams.h (72 bytes)
 RAY_RECORD = np.dtype([("src", "<i4"), ("dst", "<i4"), ("path", "<i4"), ("traced", "<i4"),
                        ("successful", "<i4"), ("hit_cnt", "<i4"), ("launch_angle", "<f4"),
                        ("receive_angle", "<f4"), ("loss", "<f4"), ("pad0", "<f4"),
                        ("phase", "<f8"), ("hit_loss_idx", "<i4", 5), ("pad1", "<i4")])
-assert RAY_RECORD.itemsize == 64
+assert RAY_RECORD.itemsize == 72
 
 
 def sort_paths(paths):

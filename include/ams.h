@@ -135,7 +135,7 @@ typedef struct {
   double phase;
   int32_t hit_loss_idx[5];
   int32_t pad1;
-} ams_ray_record; /* 64 bytes */
+} ams_ray_record; /* 72 bytes */
 
 /* ams_trace_channel, and every backward ray of stage 2 written to records
  * (device, capacity max_records; rays past it are counted, not written) in
