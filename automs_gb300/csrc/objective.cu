@@ -856,16 +856,37 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
   constexpr int NW = 32;
   // a bounded wait of the streaming kernel ran out: its partials are
   // incomplete, so every output of the call is NaN
-  const bool bad = obj_failed(err);
   const int K = M + a.S;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + lane;
+  // call inputs (not written by the streaming grid) are fetched before the
+  // wait: this warp's first H_a row for the dL/dW part and phi for the phase
+  const c2 ha_first = warp < a.S && k < M ? ld2(a.Ha, (size_t)warp * M + k) : c2{0.f, 0.f};
+  const float phi_k = warp == 0 && k < M ? __ldg(a.phi + k) : 0.f;
+  // launched early (programmatic dependent launch): wait for the streaming
+  // grid to complete before reading its partials or its wait-timeout word
+  cudaGridDependencySynchronize();
+  const bool bad = obj_failed(err);
   __shared__ float inv_s;
   __shared__ c2 r1[NW][CB][32], r2[NW][CB][32];
   __shared__ c2 gv[CB][32];
-  if (warp == 0) {
+  // Every loop below issues a batch of UNR independent loads before adding
+  // them (in the same order as one load per iteration would), so a warp pays
+  // one memory round trip per batch rather than one per partial.
+  constexpr int UNR = 8;
+  if (warp == 1) {
     double x = 0.0, z = 0.0;
-    for (int b = lane; b < nparts; b += 32) { x += lpart[2 * b]; z += lpart[2 * b + 1]; }
+    for (int b0 = lane; b0 < nparts; b0 += 32 * UNR) {
+      double xv[UNR], zv[UNR];
+#pragma unroll
+      for (int u = 0; u < UNR; u++) {
+        const int b = b0 + 32 * u;
+        xv[u] = b < nparts ? lpart[2 * b] : 0.0;
+        zv[u] = b < nparts ? lpart[2 * b + 1] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < UNR; u++) { x += xv[u]; z += zv[u]; }
+    }
     for (int o = 16; o > 0; o >>= 1) {
       x += __shfl_xor_sync(0xffffffffu, x, o);
       z += __shfl_xor_sync(0xffffffffu, z, o);
@@ -881,18 +902,32 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
   c2 s1[CB], s2[CB];
 #pragma unroll
   for (int c = 0; c < CB; c++) { s1[c] = {0.f, 0.f}; s2[c] = {0.f, 0.f}; }
-#pragma unroll 4
-  for (int b = warp; b < nparts; b += NW) {
+  constexpr int UNP = UNR / CB;  // partial loads per batch (registers)
+  for (int b0 = warp; b0 < nparts; b0 += NW * UNP) {
+    float2 pu[UNP][CB], pv[UNP][CB];
 #pragma unroll
-    for (int c = 0; c < CB; c++) {
-      if (c >= a.C) continue;
-      const float2 u = __ldg(P + ((size_t)b * 2 * a.C + c) * K + kk);
-      s1[c].x += u.x;
-      s1[c].y += u.y;
-      if (CB > 1) {
-        const float2 v = __ldg(P + ((size_t)b * 2 * a.C + a.C + c) * K + kk);
-        s2[c].x += v.x;
-        s2[c].y += v.y;
+    for (int u = 0; u < UNP; u++) {
+      const int b = b0 + NW * u;
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        const bool on = b < nparts && c < a.C;
+        pu[u][c] = on ? __ldg(P + ((size_t)b * 2 * a.C + c) * K + kk) : make_float2(0.f, 0.f);
+        if (CB > 1)
+          pv[u][c] = on ? __ldg(P + ((size_t)b * 2 * a.C + a.C + c) * K + kk)
+                        : make_float2(0.f, 0.f);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < UNP; u++) {
+#pragma unroll
+      for (int c = 0; c < CB; c++) {
+        if (b0 + NW * u >= nparts || c >= a.C) continue;
+        s1[c].x += pu[u][c].x;
+        s1[c].y += pu[u][c].y;
+        if (CB > 1) {
+          s2[c].x += pv[u][c].x;
+          s2[c].y += pv[u][c].y;
+        }
       }
     }
   }
@@ -904,7 +939,7 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
     c2 e = {1.f, 0.f};
     const bool ms_row = k < M;
     if (ms_row) {
-      const float pp = py_mod(__ldg(a.phi + k), a.max_phase);
+      const float pp = py_mod(phi_k, a.max_phase);
       sincosf(pp, &e.y, &e.x);
     }
     float dph = 0.f;
@@ -934,7 +969,7 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
   if (!a.grad_W) return;
   __syncthreads();
   for (int s2 = warp; s2 < a.S; s2 += NW) {
-    const c2 h = k < M ? ld2(a.Ha, (size_t)s2 * M + k) : c2{0.f, 0.f};
+    const c2 h = s2 == warp ? ha_first : k < M ? ld2(a.Ha, (size_t)s2 * M + k) : c2{0.f, 0.f};
 #pragma unroll
     for (int c = 0; c < CB; c++) {
       if (c >= a.C) continue;
@@ -960,6 +995,7 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
   __threadfence();
   for (int i = warp; i < a.C * a.S; i += NW) {
     const int c = i / a.S, s2 = i % a.S;
+    const float2 g = __ldcg(reinterpret_cast<const float2 *>(GU) + (size_t)c * K + M + s2);
     c2 acc = {0.f, 0.f};
     for (int b = lane; b < (int)gridDim.x; b += 32) {
       const float2 v = __ldcg(reinterpret_cast<const float2 *>(dwp) + (size_t)b * a.C * a.S + i);
@@ -971,7 +1007,6 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
       acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
     }
     if (lane == 0) {
-      const float2 g = __ldcg(reinterpret_cast<const float2 *>(GU) + (size_t)c * K + M + s2);
       reinterpret_cast<float2 *>(a.grad_W)[i] =
           bad ? make_float2(obj_nan(), obj_nan()) : make_float2(g.x + acc.x, g.y + acc.y);
     }
@@ -1077,6 +1112,29 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
   return tc::mbar_wait(bar, parity);
 }
 
+// the coefficients of the virtual rows into shared memory, coef[k][c]: U for
+// metasurface rows, W for the H_d rows.  Four loads per thread are issued
+// before their stores, so the staging costs one memory round trip per four
+// rows instead of one per row.
+template <int NTH, int CB>
+__device__ __forceinline__ void stage_coef(const ObjArgs &a, int M, int K, const float *U,
+                                           c2 *coef) {
+  const int n = K * CB;
+  for (int i0 = threadIdx.x; i0 < n; i0 += 4 * NTH) {
+    c2 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int i = i0 + u * NTH, k = i / CB, c = i % CB;
+      v[u] = {0.f, 0.f};
+      if (i < n && c < a.C)
+        v[u] = k < M ? ld2(U, (size_t)c * M + k) : ld2(a.W, (size_t)c * a.S + (k - M));
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (i0 + u * NTH < n) coef[i0 + u * NTH] = v[u];
+  }
+}
+
 template <int CB, int TR, int KPT>
 __global__ void __launch_bounds__(256, 2)
     k_obj_stream(ObjArgs a, const __grid_constant__ CUtensorMap mapR,
@@ -1129,12 +1187,7 @@ __global__ void __launch_bounds__(256, 2)
   // the first tiles are in flight; wait for the U kernel, then stage the
   // coefficients: U for metasurface rows, W for the H_d rows
   cudaGridDependencySynchronize();
-  for (int i = t; i < K * CB; i += NTH) {
-    const int k = i / CB, c = i % CB;
-    c2 v = {0.f, 0.f};
-    if (c < a.C) v = k < M ? ld2(U, (size_t)c * M + k) : ld2(a.W, (size_t)c * a.S + (k - M));
-    coef[i] = v;
-  }
+  stage_coef<NTH, CB>(a, M, K, U, coef);
   __syncthreads();
 
   c2 p1[KPT][CB], p2[KPT][CB];
@@ -1258,6 +1311,9 @@ __global__ void __launch_bounds__(256, 2)
       if (tile + 2 * (int)gridDim.x < ntiles) issue(tile + 2 * gridDim.x, stg);
     }
   }
+  // the tail kernel may launch now; its grid-dependency wait still waits for
+  // this grid to complete, with every write below visible
+  cudaTriggerProgrammaticLaunchCompletion();
   // partials of this CTA: P1 at [b][c][k], P2 at [b][C + c][k]
 #pragma unroll
   for (int q = 0; q < KPT; q++) {
@@ -1426,8 +1482,17 @@ cudaError_t stream_tail(const ObjArgs &a, int M, int nparts, const float *U, con
                         const double *lp, float *GU, float *dwp, unsigned *counter,
                         const unsigned *err, cudaStream_t st) {
   const int K = M + a.S, nblk = (K + 31) / 32;
-  k_stream_tail<CB><<<nblk, 1024, 0, st>>>(a, M, nparts, Pp, lp, U, GU, dwp, counter, err);
-  return cudaGetLastError();
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblk);
+  cfg.blockDim = dim3(1024);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_stream_tail<CB>, a, M, nparts, Pp, lp, U, GU, dwp, counter,
+                            err);
 }
 
 // ------------------------------------------------------------------
@@ -1495,12 +1560,7 @@ __global__ void __launch_bounds__(256)
     if (first + (int)gridDim.x < ntiles) issue(first + gridDim.x, 1);
   }
   cudaGridDependencySynchronize();
-  for (int i = t; i < K * CB; i += NTH) {
-    const int k = i / CB, c = i % CB;
-    c2 v = {0.f, 0.f};
-    if (c < a.C) v = k < M ? ld2(U, (size_t)c * M + k) : ld2(a.W, (size_t)c * a.S + (k - M));
-    coef[i] = v;
-  }
+  stage_coef<NTH, CB>(a, M, K, U, coef);
   __syncthreads();
 
   c2 p1[KPT][CB], p2[KPT][CB];
@@ -1623,6 +1683,9 @@ __global__ void __launch_bounds__(256)
       if (tile + 2 * (int)gridDim.x < ntiles) issue(tile + 2 * gridDim.x, stg);
     }
   }
+  // the tail kernel may launch now; its grid-dependency wait still waits for
+  // this grid to complete, with every write below visible
+  cudaTriggerProgrammaticLaunchCompletion();
 #pragma unroll
   for (int q = 0; q < KPT; q++) {
     const int k = t + NTH * q;
