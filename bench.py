@@ -450,7 +450,7 @@ def surrogate_bench(torch, n_train=1500, n_val=200, n_cand=5000, top_frac=0.05, 
     """Surrogate-screened placement search against the plain tracer-judged
     annealing loop (placement.TwoRoomStudy: 16 seeded two-room floors, AP in
     room A before the door, 64x64 Rx over room B, metasurfaces of 16x16 to
-    48x48 on room B's walls; a sample = the three traces + 12 Adam steps of
+    48x48 on room A's other walls relaying through the door; a sample = the three traces + 12 Adam steps of
     the phase map; target = the 64x64 gain map in dB).  The MLP
     72 -> 4x512 -> 4096 (BF16 tcgen05 GEMMs, FP32 master weights) trains on
     n_train traced samples and is scored on n_val others against the
@@ -529,7 +529,7 @@ def surrogate_bench(torch, n_train=1500, n_val=200, n_cand=5000, top_frac=0.05, 
             "best_gain_db_screened_vs_plain": [[r["screened_best_db"], r["plain_best_db"]]
                                                for r in rows],
             "config": {"workload": "two-room NLOS study: 16 floors, 64x64 Rx in room B, "
-                                   "MS 16x16-48x48 on room B walls, MLP 72-4x512-4096",
+                                   "MS 16x16-48x48 on room A walls, MLP 72-4x512-4096",
                        "train_samples": n_train, "val_samples": n_val, "candidates": n_cand,
                        "judged_per_scene": rows[0]["judged"], "t_trial_s": t_trial,
                        "t_fit_s": t_fit, "fit_loss_first_last": [hist[0], hist[-1]]}}
