@@ -450,8 +450,9 @@ def surrogate_bench(torch, n_train=1500, n_val=200, n_cand=5000, top_frac=0.05, 
     """Surrogate-screened placement search against the plain tracer-judged
     annealing loop (placement.TwoRoomStudy: 16 seeded two-room floors, AP in
     room A before the door, 64x64 Rx over room B, metasurfaces of 16x16 to
-    48x48 on room A's other walls relaying through the door; a sample = the three traces + 12 Adam steps of
-    the phase map; target = the 64x64 gain map in dB).  The MLP
+    48x48 on room A's other walls relaying through the door; a sample = the
+    three traces + 12 Adam steps of the phase map; target = the 64x64 gain
+    map in dB).  The MLP
     72 -> 4x512 -> 4096 (BF16 tcgen05 GEMMs, FP32 master weights) trains on
     n_train traced samples and is scored on n_val others against the
     constant-mean predictor.  Then per test scene, from one random start: a
