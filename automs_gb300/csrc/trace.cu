@@ -326,21 +326,22 @@ __device__ void traverse(const BvhNode *nodes, const float4 *prims, int n, const
   }
 }
 
-// optixTrace with a visibility mask: bit i selects instance i (0 scene,
-// 1 Tx spheres, 2 Rx spheres), optixPathTracer.cpp:417-424
-__device__ __forceinline__ Hit closest(const TraceDev &P, af3 o, af3 d, int mask) {
+// Backward-ray query of stage 2: optixTrace with the visibility mask of the
+// scene and the Tx spheres (optixPathTracer.cpp:417-424).  On a path's last
+// segment the Tx sphere is the expected hit: finding it first bounds the
+// scene traversal to the segment before it instead of the wall behind the
+// Tx.  Other segments end on a triangle, so the scene goes first there.  The
+// result is the same lexicographic minimum in either order.
+__device__ __forceinline__ Hit closest_s2(const TraceDev &P, af3 o, af3 d, bool last) {
   RayT r;
   ray_setup(r, o, d);
   Hit h;
   h.t = AMS_TMAX; h.inst = 3; h.prim = 0x7fffffff;
-  // The result is the lexicographic minimum of (t, instance, primitive) over
-  // all primitives, so the order of the traversals changes nothing but the
-  // work: Rx spheres first (most forward segments end a few cm ahead on one),
-  // then the scene pruned at that distance.  (A per-segment choice of order
-  // measured slower: two inlined copies of the sphere traversal.)
-  if (mask & 4) traverse<2>(P.rx_nodes, P.rx_prims, P.n_dst, r, h, P.dst_r, P.err);
-  if (mask & 1) traverse<0>(P.tri_nodes, P.tri_prims, P.n_tri, r, h, 0.0f, P.err);
-  if (mask & 2) traverse<1>(P.tx_nodes, P.tx_prims, P.n_src, r, h, P.src_r, P.err);
+#pragma unroll 1
+  for (int ph = 0; ph < 2; ph++) {
+    if ((ph == 0) == last) traverse<1>(P.tx_nodes, P.tx_prims, P.n_src, r, h, P.src_r, P.err);
+    else traverse<0>(P.tri_nodes, P.tri_prims, P.n_tri, r, h, 0.0f, P.err);
+  }
   return h;
 }
 
@@ -1004,7 +1005,7 @@ __device__ __forceinline__ bool s2_ray(const TraceDev &P, int slot, int s, af3 o
   bool ok = false;
   while (ttl > 0) {
     if (++guard > AMS_SEG_CAP) { atomicOr(P.err, AMS_DERR_LOOP); break; }
-    Hit h = closest(P, o, d, 3);
+    Hit h = closest_s2(P, o, d, ttl == 1);
     segs++;
     if (h.inst == 3) break;
     const float t = h.t;
