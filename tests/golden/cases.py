@@ -16,7 +16,14 @@ STAT_KEYS = ("rx_paths", "rx_fail", "fwd_records", "unique_records", "unique_pat
 
 CHANNEL_CASES = ("tiny", "small", "pen_l3", "allpen_l4", "ms_to_rx", "ap_to_ms",
                  "bp3_door", "spl2_cap", "l0", "l5", "ms3_ap_rx", "ms3_ap_ms", "ms3_ms_rx",
-                 "farfield")
+                 "farfield", "empty_scene", "one_tri", "one_rx", "reserve1", "ragged",
+                 "rx_row")
+
+# edge cases on the tiny room: no triangles (free space), a single triangle
+# (the hierarchy is one leaf), a single Rx, the smallest record cap with four
+# samples per launch (the cap binds), an Rx grid that the grid cell size
+# divides in neither direction, and a one-row Rx grid
+_EDGE = ("empty_scene", "one_tri", "one_rx", "reserve1", "ragged", "rx_row")
 
 # the three traces of the small one-metasurface channel set
 _MS3 = {"ms3_ap_rx": "src_to_dst", "ms3_ap_ms": "src_to_ms{0}", "ms3_ms_rx": "ms{0}_to_dst"}
@@ -45,7 +52,7 @@ def channel_case(name):
         return dict(tris=tris, mat=mat, mat_prop=mp, src=t["src"], dst=t["dst"],
                     params=dict(t["params"]))
     if name in ("tiny", "pen_l3", "allpen_l4", "ms_to_rx", "bp3_door", "spl2_cap", "l0", "l5",
-                "farfield"):
+                "farfield") + _EDGE:
         c = scenes.coverage_config("coverage-tiny")
     elif name in ("small", "ap_to_ms"):
         c = scenes.coverage_config("coverage-small")
@@ -87,6 +94,23 @@ def channel_case(name):
         # of metre-sized triangles: the FSPL then splits at that hit.
         p["wave_len"] = 20.0
         p["max_reflection"] = 3
+    elif name == "empty_scene":
+        c["tris"] = np.zeros((0, 3, 3), np.float32)
+        c["mat"] = np.zeros(0, np.int32)
+    elif name == "one_tri":
+        c["tris"] = np.ascontiguousarray(c["tris"].reshape(-1, 3, 3)[:1])
+        c["mat"] = np.ascontiguousarray(c["mat"][:1])
+    elif name == "one_rx":
+        c["dst"] = np.ascontiguousarray(c["dst"][3:4, 5:6])
+        p["launch_x"] = p["launch_y"] = 300
+    elif name == "reserve1":
+        p["reserve_size"] = 1
+        p["samples_per_launch"] = 4
+        p["launch_x"] = p["launch_y"] = 32
+    elif name == "ragged":
+        c["dst"] = np.ascontiguousarray(c["dst"][:7, :13])
+    elif name == "rx_row":
+        c["dst"] = np.ascontiguousarray(c["dst"][:1])
     elif name == "l5":
         c["mat_prop"][3:] *= -1
         p["max_reflection"] = 5
