@@ -1070,13 +1070,17 @@ __device__ __forceinline__ bool s2_ray(const TraceDev &P, int slot, int s, af3 o
     ph = ph - 6.283185307179586 * floor(ph * 0.15915494309189535);
     float sn, cs;
     sincosf((float)ph, &sn, &cs);
-    double re = (double)(amp * cs), im = (double)(-amp * sn);
-    if (!(fabs(re) < AMS_ACC_LIMIT && fabs(im) < AMS_ACC_LIMIT)) {
+    // the contribution in 2^-56 fixed point, in FP32: the limit (64) and the
+    // scale (2^56) are powers of two, so the range test and the scaling are
+    // exact in float and the rounding to an integer sees the same value as
+    // a conversion through double would (FP64 is slow on this part)
+    const float re = amp * cs, im = -amp * sn;
+    if (!(fabsf(re) < (float)AMS_ACC_LIMIT && fabsf(im) < (float)AMS_ACC_LIMIT)) {
       atomicOr(P.err, AMS_DERR_ACC_RANGE);
       return false;
     }
-    cre = (unsigned long long)__double2ll_rn(re * AMS_ACC_SCALE);
-    cim = (unsigned long long)__double2ll_rn(im * AMS_ACC_SCALE);
+    cre = (unsigned long long)__float2ll_rn(re * (float)AMS_ACC_SCALE);
+    cim = (unsigned long long)__float2ll_rn(im * (float)AMS_ACC_SCALE);
   }
   return ok;
 }
