@@ -179,6 +179,12 @@ class TwoRoomStudy:
     situation of the reference's trial (a metasurface lighting the area a
     wall-mounted AP covers poorly, physical_exp_nni_model.py:26-87).
 
+    With max_reflection = 1 most of room B has no path from the AP at all
+    (57% of the cells of the 16 floors of seed 3) and sits at the coverage
+    floor, so a placement that relays through the door gains tens of dB
+    there; with 2 the AP reaches most cells within two bounces and the
+    gains are small.
+
     A placement is p = (scene, wall, u, v, n): the scene of the pool, the
     wall (0: back wall x = 0, 1: side y = 0, 2: side y = d, both over room
     A), the position along it and the height as fractions, and the side in
