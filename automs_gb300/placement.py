@@ -316,41 +316,95 @@ class TwoRoomStudy:
     def evaluate(self, p, return_detail=False):
         """Trace + optimise one placement; returns its gain map (dB over the
         Rx grid, with the optimised metasurface minus without)."""
+        return self._evaluate_on(p, self.scenes[int(p[0])]["scene"], None, return_detail)
+
+    def _evaluate_on(self, p, scene, obj_lock, return_detail=False):
         e = self.scenes[int(p[0])]
         pos, quad, nrm = self.ms_geometry(p)
         sc = tracer.Scene(*scenes.with_blackholes(e["tris"], e["mat"], e["mat_prop"], [quad]))
         Hd, _ = self._trace(sc, e["src"], e["dst"], 2, 0, (1, 0, 0), (0, 0, 0))
         sc.close()
-        Ha, _ = self._trace(e["scene"], e["src"], pos, 2, 1, (1, 0, 0), nrm)
-        Hr, _ = self._trace(e["scene"], pos, e["dst"], 1, 0, nrm, (0, 0, 0))
+        Ha, _ = self._trace(scene, e["src"], pos, 2, 1, (1, 0, 0), nrm)
+        Hr, _ = self._trace(scene, pos, e["dst"], 1, 0, nrm, (0, 0, 0))
         M = pos.shape[0] * pos.shape[1]
-        phi = torch.zeros(M, device="cuda", requires_grad=True)
-        opt = torch.optim.Adam([phi], lr=0.3)
         R = Hd.shape[1]
-        for _ in range(self.opt_steps):
-            loss = objective.capacity_objective(self.W, Hd, Ha, Hr, phi, 2 * math.pi, 1.0 / R)
-            loss.backward()
-            opt.step()
-            opt.zero_grad()
-        with torch.no_grad():
-            _, recv = objective.capacity_objective(self.W, Hd, Ha, Hr, phi.detach(), 2 * math.pi,
-                                                   1.0 / R, return_recv=True)
-            db = (20 * torch.log10(recv[0] + 1e-12)).clamp_min(self.FLOOR_DB).reshape(-1)
-            gain = db - e["db0"]
+        # the objective's scratch is per device: concurrent placements run
+        # their optimisation one at a time, each finished before the next
+        if obj_lock is not None:
+            obj_lock.acquire()
+        try:
+            phi = torch.zeros(M, device="cuda", requires_grad=True)
+            opt = torch.optim.Adam([phi], lr=0.3)
+            for _ in range(self.opt_steps):
+                loss = objective.capacity_objective(self.W, Hd, Ha, Hr, phi, 2 * math.pi, 1.0 / R)
+                loss.backward()
+                opt.step()
+                opt.zero_grad()
+            with torch.no_grad():
+                _, recv = objective.capacity_objective(self.W, Hd, Ha, Hr, phi.detach(),
+                                                       2 * math.pi, 1.0 / R, return_recv=True)
+                db = (20 * torch.log10(recv[0] + 1e-12)).clamp_min(self.FLOOR_DB).reshape(-1)
+                gain = db - e["db0"]
+            if obj_lock is not None:
+                torch.cuda.current_stream().synchronize()
+        finally:
+            if obj_lock is not None:
+                obj_lock.release()
         if return_detail:
             return gain, dict(phi=phi.detach())
         return gain
 
-    def dataset(self, n, seed=0, log=None, scene=None):
+    def evaluate_many(self, ps, workers=4):
+        """evaluate() of several placements at once, results equal to one at
+        a time: `workers` host threads, each with its own CUDA stream and
+        its own scene handles, so that one placement's traces (and their
+        flood-fill round trips) overlap the others'; the optimisation steps
+        of one placement at a time.  The plain annealing loop cannot do
+        this (each move waits for the last one's result); a screened search
+        knows the placements it will judge in advance."""
+        import concurrent.futures as cf
+        import threading
+        local = threading.local()
+        made, lock, obj_lock = [], threading.Lock(), threading.Lock()
+
+        def work(p):
+            if not hasattr(local, "stream"):
+                local.stream, local.scenes = torch.cuda.Stream(), {}
+            k = int(p[0])
+            with torch.cuda.stream(local.stream):
+                if k not in local.scenes:
+                    e = self.scenes[k]
+                    local.scenes[k] = tracer.Scene(e["tris"], e["mat"], e["mat_prop"])
+                    with lock:
+                        made.append(local.scenes[k])
+                g = self._evaluate_on(p, local.scenes[k], obj_lock)
+                local.stream.synchronize()
+                return g
+
+        torch.cuda.synchronize()
+        try:
+            with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+                out = list(ex.map(work, ps))
+        finally:
+            torch.cuda.synchronize()
+            for s_ in made:
+                s_.close()
+        return out
+
+    def dataset(self, n, seed=0, log=None, scene=None, workers=1):
+        """n seeded random placements with their descriptors and traced gain
+        maps; with workers > 1 traced by evaluate_many (same results)."""
         rng = np.random.Generator(np.random.PCG64(seed))
-        X, Y, P = [], [], []
-        for i in range(n):
-            p = self.random_params(rng, scene)
-            X.append(self.descriptor(p))
-            Y.append(self.evaluate(p).float().cpu().numpy())
-            P.append(p)
-            if log and (i + 1) % 200 == 0:
-                log(f"{i + 1}/{n} samples")
+        P = [self.random_params(rng, scene) for _ in range(n)]
+        X = [self.descriptor(p) for p in P]
+        if workers > 1:
+            Y = [g.float().cpu().numpy() for g in self.evaluate_many(P, workers)]
+        else:
+            Y = []
+            for i, p in enumerate(P):
+                Y.append(self.evaluate(p).float().cpu().numpy())
+                if log and (i + 1) % 200 == 0:
+                    log(f"{i + 1}/{n} samples")
         return np.stack(X), np.stack(Y), P
 
     def close(self):

@@ -50,8 +50,14 @@ def test_surrogate_learns_the_lit_cells():
     from automs_gb300 import placement, surrogate
     study = placement.TwoRoomStudy(n_scenes=16, seed=3, rx=(64, 64), launch=250, max_reflection=1,
                                    sizes=(32, 64))
-    Xtr, Ytr, _ = study.dataset(1500, seed=1)
-    Xva, Yva, _ = study.dataset(200, seed=2)
+    Xtr, Ytr, _ = study.dataset(1500, seed=1, workers=4)
+    Xva, Yva, _ = study.dataset(200, seed=2, workers=4)
+    # placements traced together give the gain maps of one at a time
+    rng = np.random.Generator(np.random.PCG64(9))
+    P = [study.random_params(rng) for _ in range(6)]
+    many = study.evaluate_many(P, workers=3)
+    for p, g in zip(P, many):
+        assert torch.equal(g, study.evaluate(p)), p
     study.close()
     mu, sd = Ytr.mean(0), Ytr.std() + 1e-6
     net = surrogate.MLP([Xtr.shape[1], 512, 512, 512, 512, Ytr.shape[1]], max_batch=4096, seed=0)
