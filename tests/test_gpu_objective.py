@@ -55,6 +55,47 @@ def test_fused_objective_vs_oracle(obj, name):
         np.testing.assert_allclose(gp, gphi_o, rtol=1e-3, atol=1e-3 * np.abs(gphi_o).max())
 
 
+@pytest.mark.parametrize("S,M,R,C", [(1, 1, 1, 1), (1, 0, 5, 1), (3, 5, 7, 64), (16, 64, 201, 1),
+                                     (4, 9, 33, 2), (2, 17, 4097, 3)])
+def test_objective_edge_shapes_vs_oracle(obj, S, M, R, C):
+    """Degenerate and ragged shapes through the direct call: one element
+    everywhere, no metasurface, the largest codebook (64 codes), an odd Rx
+    count (no streaming tiles: the split path), two codes (the streaming
+    path's second bucket) and a column count one past a tile, against the
+    FP64 oracle."""
+    rng = np.random.Generator(np.random.PCG64(1000 + S * 7 + M * 11 + R + C))
+    lam = 3e8 / 60e9
+
+    def cn(*sh):
+        d = rng.uniform(2.0, 15.0, size=sh)
+        g = (rng.normal(size=sh) + 1j * rng.normal(size=sh)) / np.sqrt(2)
+        return (g * lam / (4 * np.pi * d)).astype(np.complex64)
+    Hd = cn(S, R)
+    Ha, Hr = (cn(S, M), cn(M, R)) if M else (None, None)
+    phi = rng.uniform(0, 2 * np.pi, M).astype(np.float32) if M else None
+    theta = rng.uniform(0, 2 * np.pi, (C, S)).astype(np.float32)
+    A = OO.antenna_amplitude(C, S)
+    drop = np.zeros(C, bool)
+    if C > 2:
+        drop[C // 2] = True
+    mp, w = 2 * np.pi, 1.0 / R
+    loss_o, gth_o, gphi_o, ex = OO.objective(Hd, Ha, Hr, phi, theta, A, w, drop, mp)
+    th = cuda(theta).requires_grad_(True)
+    W = cuda(A.astype(np.float32)) * torch.exp(-1j * th)
+    ph = cuda(phi).requires_grad_(True) if M else None
+    loss, recv = obj.capacity_objective(W, cuda(Hd), cuda(Ha) if M else None,
+                                        cuda(Hr) if M else None, ph, mp, w, cuda(drop),
+                                        return_recv=True)
+    loss.backward()
+    np.testing.assert_allclose(float(loss), loss_o, rtol=1e-4, atol=1e-6)
+    np.testing.assert_allclose(recv.cpu().numpy(), ex["amp"], rtol=1e-4, atol=1e-9)
+    g = th.grad.cpu().numpy()
+    np.testing.assert_allclose(g, gth_o, rtol=1e-3, atol=1e-3 * np.abs(gth_o).max() + 1e-12)
+    if M:
+        gp = ph.grad.cpu().numpy()
+        np.testing.assert_allclose(gp, gphi_o, rtol=1e-3, atol=1e-3 * np.abs(gphi_o).max() + 1e-12)
+
+
 @pytest.mark.parametrize("name", cases.OBJECTIVE_CASES)
 def test_model_matches_reference_model(obj, name):
     """automs_gb300.objective.Model against go.Model run by the reference
