@@ -89,11 +89,14 @@ def test_objective_edge_shapes_vs_oracle(obj, S, M, R, C):
     loss.backward()
     np.testing.assert_allclose(float(loss), loss_o, rtol=1e-4, atol=1e-6)
     np.testing.assert_allclose(recv.cpu().numpy(), ex["amp"], rtol=1e-4, atol=1e-9)
+    # with one AP element |Y| does not depend on theta: the exact gradient is
+    # zero and FP32 leaves rounding noise of the loss's scale times 2^-24
+    floor = 1e-6 * max(1.0, abs(loss_o))
     g = th.grad.cpu().numpy()
-    np.testing.assert_allclose(g, gth_o, rtol=1e-3, atol=1e-3 * np.abs(gth_o).max() + 1e-12)
+    np.testing.assert_allclose(g, gth_o, rtol=1e-3, atol=1e-3 * np.abs(gth_o).max() + floor)
     if M:
         gp = ph.grad.cpu().numpy()
-        np.testing.assert_allclose(gp, gphi_o, rtol=1e-3, atol=1e-3 * np.abs(gphi_o).max() + 1e-12)
+        np.testing.assert_allclose(gp, gphi_o, rtol=1e-3, atol=1e-3 * np.abs(gphi_o).max() + floor)
 
 
 @pytest.mark.parametrize("name", cases.OBJECTIVE_CASES)
