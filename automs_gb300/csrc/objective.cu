@@ -854,8 +854,6 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
                                                       const float *U, float *GU, float *dwp,
                                                       unsigned *counter, const unsigned *err) {
   constexpr int NW = 32;
-  // a bounded wait of the streaming kernel ran out: its partials are
-  // incomplete, so every output of the call is NaN
   const int K = M + a.S;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int k = blockIdx.x * 32 + lane;
@@ -866,6 +864,8 @@ __global__ void __launch_bounds__(1024) k_stream_tail(ObjArgs a, int M, int npar
   // launched early (programmatic dependent launch): wait for the streaming
   // grid to complete before reading its partials or its wait-timeout word
   cudaGridDependencySynchronize();
+  // a bounded wait of the streaming kernel ran out: its partials are
+  // incomplete, so every output of the call is NaN
   const bool bad = obj_failed(err);
   __shared__ float inv_s;
   __shared__ c2 r1[NW][CB][32], r2[NW][CB][32];
