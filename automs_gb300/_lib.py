@@ -41,7 +41,7 @@ class Stats(C.Structure):
         ("ms_bvh", C.c_float), ("ms_stage1", C.c_float), ("ms_stage2", C.c_float),
         ("ms_total", C.c_float), ("workspace_bytes", C.c_ulonglong),
         ("segments_fwd", C.c_ulonglong), ("segments_bwd", C.c_ulonglong),
-        ("ms_stage2_kernel", C.c_float),
+        ("ms_stage2_kernel", C.c_float), ("acc_adds", C.c_ulonglong),
     ]
 
     def as_dict(self):

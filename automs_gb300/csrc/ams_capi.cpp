@@ -566,6 +566,7 @@ ams_status trace_impl(ams_scene *S, const ams_trace_params *p, const float *src,
       stats->segments_fwd = S->hc->ctr[8];
       stats->segments_bwd = S->hc->ctr[9];
       stats->ms_stage2_kernel = ms_k2;
+      stats->acc_adds = S->hc->ctr[13];
     }
     if (n_records) *n_records = P.rec_base;
     if (p->log_level > 0) {

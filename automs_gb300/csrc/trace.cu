@@ -1106,7 +1106,7 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
   const int lane = threadIdx.x & 31;
   const af3 srcdir = mk3(P.src_dir[0], P.src_dir[1], P.src_dir[2]);
   const af3 dstdir = mk3(P.dst_dir[0], P.dst_dir[1], P.dst_dir[2]);
-  unsigned n_ok = 0, n_fail = 0, n_segs = 0;
+  unsigned n_ok = 0, n_fail = 0, n_segs = 0, n_adds = 0;  // n_adds: warp total
   if (blockIdx.x == 0 && threadIdx.x == 0 && n_items > (long long)gridDim.x * (blockDim.x >> 5))
     atomicOr(P.err, AMS_DERR_TASKS);  // the launch must cover every item
   {
@@ -1143,11 +1143,13 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
       if (__any_sync(0xffffffffu, ok) && lane == 0)
         atomicOr(P.S + (size_t)cell * P.W + (path >> 5), 1u << (path & 31));
     }
-    if (act && (sre | sim)) {
+    const bool add = act && (sre | sim);
+    if (add) {
       unsigned long long *acc = P.acc + ((size_t)dst * S + s) * 2;
       atomicAdd(acc, sre);
       atomicAdd(acc + 1, sim);
     }
+    n_adds += 2u * (unsigned)__popc(__ballot_sync(0xffffffffu, add));
   }
   for (int off = 16; off > 0; off >>= 1) {
     n_ok += __shfl_xor_sync(0xffffffffu, n_ok, off);
@@ -1155,6 +1157,7 @@ __global__ void __launch_bounds__(256, 5) k_stage2(TraceDev P) {
     n_segs += __shfl_xor_sync(0xffffffffu, n_segs, off);
   }
   if (lane == 0) {
+    if (n_adds) atomicAdd(P.ctr + 13, (unsigned long long)n_adds);
     if (n_segs) atomicAdd(P.ctr + 9, (unsigned long long)n_segs);
     if (n_ok) atomicAdd(P.ctr + 3, (unsigned long long)n_ok);
     if (n_fail) atomicAdd(P.ctr + 4, (unsigned long long)n_fail);
@@ -1234,7 +1237,10 @@ __global__ void __launch_bounds__(256, 5) k_stage2_rays(TraceDev P) {
   for (int off = 16; off > 0; off >>= 1) segs += __shfl_xor_sync(0xffffffffu, segs, off);
   if (lane == 0) {
     if (segs) atomicAdd(P.ctr + 9, (unsigned long long)segs);
-    if (okb) atomicAdd(P.ctr + 3, (unsigned long long)__popc(okb));
+    if (okb) {
+      atomicAdd(P.ctr + 3, (unsigned long long)__popc(okb));
+      atomicAdd(P.ctr + 13, 2ull * (unsigned long long)__popc(okb));  // two adds per ray
+    }
     if (trb & ~okb) atomicAdd(P.ctr + 4, (unsigned long long)__popc(trb & ~okb));
   }
   const unsigned same = __match_any_sync(0xffffffffu, t);

@@ -73,7 +73,7 @@ struct TraceDev {
   // counters: 0 records, 1 overflow threads, 2 occupied slots, 3 ok rays,
   // 4 failed rays, 5 tasks this round, 6 unique records, 7 new tasks,
   // 8 stage-1 closest-hit queries, 9 stage-2 closest-hit queries,
-  // 10 stage-1 launch-index fetch, 12 dense path ids
+  // 10 stage-1 launch-index fetch, 12 dense path ids, 13 int64 adds into acc
   unsigned long long *ctr;
   unsigned *err;
   // per-ray records of stage 2 (ams_trace_channel_export): record of ray r

@@ -630,7 +630,9 @@ def channel_ms_bench(torch, warmup, steps, flush):
         ms = sum(a for a, _ in v) / len(v)
         st = v[0][1]
         traces[key] = {"ms": round(ms, 2), "rx_paths": st["rx_paths"],
-                       "ms_stage2": round(st["ms_stage2"], 2)}
+                       "ms_stage2": round(st["ms_stage2"], 2),
+                       "acc_adds_per_verified_ray": (round(st["acc_adds"] / st["rx_paths"], 3)
+                                                     if st["rx_paths"] else None)}
         tot_ms += ms
         tot_paths += st["rx_paths"]
     # objective + adjoint on the traced channels, reference orientation
@@ -881,7 +883,9 @@ def main():
                          "peak_kind": f"{n_sm} SM x 128 lanes x 2 at the sampled SM clock"},
         "roofline_stage2": {"bound": "hbm", "kernel": "k_stage2", "achieved": gbs2, "peak": hbm,
                             "unit": "GB/s", "frac": gbs2 / hbm, "traffic": stage2_traffic(),
-                            "peak_kind": peak_kind, "algorithmic_bytes": alg2},
+                            "peak_kind": peak_kind, "algorithmic_bytes": alg2,
+                            "acc_adds_per_verified_ray": (st0["acc_adds"] / succ if succ
+                                                          else None)},
         "roofline_stage2_alu": {"bound": "fp32", "kernel": "k_stage2", "achieved": tfl2,
                                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": tfl2 / fp32_peak,
                                 "flop_per_segment": FLOP_PER_SEGMENT,

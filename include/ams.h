@@ -73,6 +73,10 @@ typedef struct {
   unsigned long long segments_fwd;   /* closest-hit queries of stage 1 */
   unsigned long long segments_bwd;   /* closest-hit queries of stage 2 */
   float ms_stage2_kernel;            /* device time of the backward kernels */
+  unsigned long long acc_adds;       /* int64 atomic adds into the fixed-point H:
+                                        two per verified ray in rounds of one
+                                        path per item, two per (Tx, Rx) pair
+                                        and chunk of paths otherwise */
 } ams_stats;
 
 /* Create a scene from device arrays: tris [n_tri*9] float (3 vertices per

@@ -43,6 +43,10 @@ def test_channel_parity_with_oracle(tracer, name):
                                       c["params"])
     for k in cases.STAT_KEYS + ("tasks", "overflow"):
         assert st[k] == so[k], (k, st[k], so[k])
+    # int64 adds into H: two per verified ray at most (fewer when a round
+    # sums several paths per (Tx, Rx) pair before adding)
+    assert st["acc_adds"] <= 2 * st["rx_paths"]
+    assert (st["acc_adds"] > 0) == (st["rx_paths"] > 0)
     assert np.array_equal(paths, po)
     # same ray set; the phase is FP64 on both sides, sin/cos differ in the last bits
     assert np.array_equal(H != 0, Ho != 0)
