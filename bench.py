@@ -471,9 +471,12 @@ def surrogate_bench(torch, n_train=1500, n_val=200, n_cand=5000, top_frac=0.05, 
     Xva, Yva, _ = study.dataset(n_val, seed=2, workers=4)
     mu, sd = Ytr.mean(0), Ytr.std() + 1e-6
     net = surrogate.MLP([Xtr.shape[1], 512, 512, 512, 512, Ytr.shape[1]], max_batch=4096, seed=0)
+    # about the same number of optimiser steps and the same final learning
+    # rate whatever the training-set size (400 epochs at 1,500 samples)
+    epochs = max(60, round(400 * 1500 / n_train))
     t0 = time.perf_counter()
     hist = net.fit(torch.as_tensor(Xtr).cuda(), torch.as_tensor((Ytr - mu) / sd).cuda(),
-                   epochs=400, batch=64, lr=1e-3, lr_decay=0.995)
+                   epochs=epochs, batch=64, lr=1e-3, lr_decay=0.995 ** (400 / epochs))
     torch.cuda.synchronize()
     t_fit = time.perf_counter() - t0
     mu_t = torch.as_tensor(mu, device="cuda")
@@ -553,7 +556,8 @@ def surrogate_bench(torch, n_train=1500, n_val=200, n_cand=5000, top_frac=0.05, 
                                 "another",
                        "t_rank_judge_plain_s": [[r["t_rank_s"], r["t_judge_s"], r["t_plain_s"]]
                                                 for r in rows],
-                       "t_fit_s": t_fit, "fit_loss_first_last": [hist[0], hist[-1]]}}
+                       "epochs": epochs, "t_fit_s": t_fit,
+                       "fit_loss_first_last": [hist[0], hist[-1]]}}
 
 
 def batch_bench(torch, n_place=64, workers=4, opt_steps=20):
@@ -697,6 +701,8 @@ def main():
                     help="profiling aid: run only the named timed loop")
     ap.add_argument("--batch-n", type=int, default=64, help="placements of the batch leg")
     ap.add_argument("--batch-workers", type=int, default=4)
+    ap.add_argument("--surrogate-train", type=int, default=1500,
+                    help="traced training samples of the surrogate leg")
     ap.add_argument("--codes-r", type=int, default=0, choices=[0, 4096, 65536],
                     help="profiling aid: run the codebook leg at one Rx count only")
     ap.add_argument("--launch", type=int, default=0,
@@ -730,7 +736,7 @@ def main():
         print(json.dumps(batch_bench(torch, n_place=args.batch_n, workers=args.batch_workers)))
         return
     if args.only == "surrogate":
-        print(json.dumps(surrogate_bench(torch)))
+        print(json.dumps(surrogate_bench(torch, n_train=args.surrogate_train)))
         return
     if args.only == "codes":
         if args.codes_r in (0, 4096):
@@ -827,7 +833,7 @@ def main():
         secondary.append(objective_codes_bench(torch, R=4096))
         secondary.append(objective_codes_bench(torch, R=65536, nset=1))
         secondary.append(channel_ms_bench(torch, 1, 1, flush))
-        secondary.append(surrogate_bench(torch))
+        secondary.append(surrogate_bench(torch, n_train=args.surrogate_train))
         secondary.append(batch_bench(torch))
 
     if rank != 0:
