@@ -61,3 +61,43 @@ def test_trace_params_validation(L):
         rc = L.ams_trace_channel(C.c_void_p(1), C.byref(p), C.c_void_p(8), 1, 1, C.c_void_p(8),
                                  1, 1, None, None, C.c_void_p(8), None, None, buf, 256)
         assert rc == 1, bad
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes and numpy mirrors of the C structs (ams_trace_params,
+    ams_stats, ams_ray_record) have the header's size and field offsets,
+    printed by a program compiled against include/ams.h."""
+    import shutil
+    import subprocess
+
+    import numpy as np
+
+    from automs_gb300 import _lib, tracer
+    if shutil.which("g++") is None:
+        pytest.skip("g++ is missing")
+    mirrors = {"ams_trace_params": _lib.TraceParams, "ams_stats": _lib.Stats}
+    lines = ['#include <cstddef>', '#include <cstdio>', '#include "ams.h"', "int main() {"]
+    for cname, py in mirrors.items():
+        lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append('  printf("ams_ray_record %zu\\n", sizeof(ams_ray_record));')
+    for f in tracer.RAY_RECORD.names:
+        lines.append(f'  printf("ams_ray_record.{f} %zu\\n", offsetof(ams_ray_record, {f}));')
+    lines.append("  return 0;\n}")
+    src = tmp_path / "layout.cpp"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                        exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = dict(line.split() for line in subprocess.run([exe], capture_output=True,
+                                                       text=True).stdout.splitlines())
+    for cname, py in mirrors.items():
+        assert int(got[cname]) == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got[f"{cname}.{f}"]) == getattr(py, f).offset, (cname, f)
+    assert int(got["ams_ray_record"]) == tracer.RAY_RECORD.itemsize
+    for f in tracer.RAY_RECORD.names:
+        assert int(got[f"ams_ray_record.{f}"]) == tracer.RAY_RECORD.fields[f][1], f
+    np.testing.assert_equal(tracer.RAY_RECORD.itemsize, 72)
