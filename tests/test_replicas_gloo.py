@@ -32,7 +32,7 @@ def _rank(rank, world, port, out):
 
 def test_two_replicas_aggregate():
     world = 2
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:  # no fork of this threaded process
         out = m.dict()
         mp.start_processes(_rank, args=(world, _free_port(), out), nprocs=world,
                            start_method="spawn")
