@@ -8,10 +8,17 @@ channel build (Tx/Rx BVH builds + stage 1 + all stage-2 rounds) on a scene
 whose triangle BVH is kept resident, as a user of the Scene API does.
 Rx-paths = successful backward verifications (the reference's stats[0]).
 
-Also reported: the plain phase-map objective (S=16, M=1024, R=4096, C=1)
-as objective+grad evals/s with its HBM roofline.
+Also reported (in "secondary"), each with its own roofline or baseline: the
+plain phase-map objective (S=16, M=1024, R=4096, C=1) as objective+grad
+evals/s; the 60-code codebook objective on tensor cores at 4,096 and 65,536
+Rx; the ms-256 channel set (50k triangles, a 32x32 metasurface, 256x256 Rx,
+3 reflections) with the objective on its traced channels; surrogate-screened
+placement annealing against the plain traced loop (two-room study); 64
+batched metasurface placements in a 200k-triangle building.  Every
+objective figure carries its error against the FP64 oracle.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--only tracer|objective|codes|ms|surrogate|batch]
 """
 import argparse
 import json
