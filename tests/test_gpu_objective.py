@@ -134,7 +134,7 @@ def test_model_matches_reference_model(obj, name):
         finally:
             torch.rand = real_rand
     loss.backward()
-    np.testing.assert_allclose(float(loss), float(g["loss"]), rtol=2e-4)
+    np.testing.assert_allclose(float(loss.detach()), float(g["loss"]), rtol=2e-4)
     gt = g["grad_theta"]
     np.testing.assert_allclose(m.antenna_theta.grad.cpu().numpy(), gt, rtol=5e-3,
                                atol=5e-3 * np.abs(gt).max())
