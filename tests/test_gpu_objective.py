@@ -159,7 +159,7 @@ def test_objective_config_size(obj):
     p = cuda(phi).requires_grad_(True)
     loss = obj.mean_capacity(w, cuda(Hd), cuda(Ha), cuda(Hr), p)
     loss.backward()
-    np.testing.assert_allclose(float(loss), loss_o, rtol=1e-5)
+    np.testing.assert_allclose(float(loss.detach()), loss_o, rtol=1e-5)
     np.testing.assert_allclose(w.grad.cpu().numpy(), gW_o, rtol=1e-3, atol=1e-3 * np.abs(gW_o).max())
     np.testing.assert_allclose(p.grad.cpu().numpy(), gphi_o, rtol=1e-3,
                                atol=1e-3 * np.abs(gphi_o).max())
@@ -290,7 +290,7 @@ def test_tensor_core_plan_matches_cuda_core_path(obj):
             loss, recv = obj.capacity_objective(Wg, Hd, Ha, Hr, pg, 2 * np.pi, 0.5, drop,
                                                 return_recv=True, plan=p)
             loss.backward()
-            outs.append((float(loss), recv, Wg.grad, pg.grad))
+            outs.append((float(loss.detach()), recv, Wg.grad, pg.grad))
         (l1, r1, w1, p1), (l2, r2, w2, p2) = outs
         assert abs(l1 - l2) <= 1e-4 * abs(l2)
         assert torch.allclose(r1, r2, rtol=1e-4, atol=1e-4 * float(r2.abs().max()))
@@ -368,7 +368,7 @@ def test_tensor_core_plan_config3_shape_vs_oracle(obj):
     obj.check_status(plan)
     amp = recv.cpu().numpy()
     g, gp = theta.grad.cpu().numpy(), ph.grad.cpu().numpy()
-    e_loss = abs(float(loss) - loss_o) / abs(loss_o)
+    e_loss = abs(float(loss.detach()) - loss_o) / abs(loss_o)
     e_amp = np.abs(amp - ex["amp"]).max() / np.abs(ex["amp"]).max()
     e_th = np.abs(g - gth_o).max() / np.abs(gth_o).max()
     e_ph = np.abs(gp - gphi_o).max() / np.abs(gphi_o).max()
@@ -398,7 +398,7 @@ def test_wait_timeout_is_reported(obj, path):
         pg = phi.clone().requires_grad_(True)
         loss = obj.capacity_objective(Wg, Hd, Ha, Hr, pg, 2 * np.pi, 1.0 / R, plan=plan)
         loss.backward()
-        return float(loss), Wg.grad.clone(), pg.grad.clone()
+        return float(loss.detach()), Wg.grad.clone(), pg.grad.clone()
     clean = run()
     obj.check_status(plan)
     lib().ams_debug_inject_wait_timeout(1)
@@ -530,7 +530,7 @@ def test_multihop_objective_vs_reference_autograd(obj):
     ref = _reference_multihop_loss(torch, t64, W64, ph, [d / 180 * np.pi for d in max_deg], 3,
                                    0.7, torch.from_numpy(drop))
     ref.backward()
-    np.testing.assert_allclose(float(loss), float(ref), rtol=1e-4)
+    np.testing.assert_allclose(float(loss.detach()), float(ref.detach()), rtol=1e-4)
     gt = th.grad.numpy()
     np.testing.assert_allclose(m.antenna_theta.grad.cpu().numpy(), gt, rtol=1e-3,
                                atol=1e-3 * np.abs(gt).max())
