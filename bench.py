@@ -315,8 +315,9 @@ def objective_bench(torch, steps, flush, cpu_baseline=False):
             OO.torch_objective_step(torch, Hd, Ha, Hr, phc, Wc, 1.0 / R)
         cpu = {"value": n_cpu / (time.perf_counter() - t0), "unit": "evals/s", "cores": threads,
                "kind": "port",
-               "sample": "20 evaluations, the reference's method (PyTorch complex64 + autograd) "
-                         "on the host CPU, same S/M/R"}
+               "sample": "20 evaluations of the reference's method restated "
+                         "(PyTorch complex64 + autograd, checked against the reference Model "
+                         "and the FP64 oracle) on the host CPU, same S/M/R"}
     bytes_alg = 8 * (R * M + M * S + R * S)
     hbm, kind = peaks()
     achieved = bytes_alg / (t * 1e-3) / 1e9
