@@ -316,8 +316,9 @@ def objective_bench(torch, steps, flush, cpu_baseline=False):
         cpu = {"value": n_cpu / (time.perf_counter() - t0), "unit": "evals/s", "cores": threads,
                "kind": "port",
                "sample": "20 evaluations of the reference's method restated "
-                         "(PyTorch complex64 + autograd, checked against the reference Model "
-                         "and the FP64 oracle) on the host CPU, same S/M/R"}
+                         "(PyTorch complex64 + autograd, checked against the FP64 oracle, "
+                         "which is pinned to the reference Model's outputs) on the host CPU, "
+                         "same S/M/R"}
     bytes_alg = 8 * (R * M + M * S + R * S)
     hbm, kind = peaks()
     achieved = bytes_alg / (t * 1e-3) / 1e9
